@@ -1,0 +1,174 @@
+/*
+ * samoa_swe.h — C ABI of the GB300-native shallow-water (SWE) time step.
+ *
+ * A drop-in for sam(oa)^2's SWE Euler time-step traversal
+ * `call swe%euler%traverse(grid)` (src/SWE/SWE.f90:393, also :339), i.e. the
+ * traversal t_swe_euler_timestep_traversal of src/SWE/SWE_euler_timestep.f90.
+ * Mesh generation, adaptivity and I/O stay on the host. After each remesh
+ * the host hands the Sierpinski-ordered cells and the edge streams to the
+ * device (swe_mesh_upload), uploads the cell state, and calls swe_traverse
+ * once per time step (or once for many steps).
+ *
+ * Conventions (all follow the reference):
+ *   - h is the water SURFACE elevation, depth = h - b (src/SWE/SWE_data_types.f90:42-65);
+ *   - cells are in the host's current traversal order; the first step after
+ *     an upload traverses them in that order, and every step reverses the
+ *     traversal direction like grid%reverse() does
+ *     (src/SFC_generic_traversal_ringbuffer.f90:420);
+ *   - local edge indices are 1 = right leg, 2 = hypotenuse, 3 = left leg in the
+ *     cell's current orientation (src/SFC_data_types.f90:47-49);
+ *   - indices are int64 like src/Generic/samoa.h; the device narrows to int32
+ *     (n_cells < 2^31).
+ * Every function returns 0 on success or a negative SWE_E* code; nothing
+ * aborts. swe_last_error() gives the message of the last failure on the
+ * calling thread. A context is not thread-safe; use one context per stream.
+ */
+#ifndef SAMOA_SWE_H
+#define SAMOA_SWE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SWE_OK 0
+#define SWE_E_INVALID -1      /* bad argument / inconsistent mesh */
+#define SWE_E_CUDA -2         /* CUDA runtime error */
+#define SWE_E_NOMESH -3       /* no mesh uploaded */
+#define SWE_E_NOMEM -4        /* device allocation failed */
+#define SWE_E_STATE -5        /* state or time step not set */
+#define SWE_E_DEVICE -6       /* a kernel reported an error (timeout, bad index) */
+
+/* flux solvers: GeoClaw numbering for the GeoClaw family
+ * (src/geoclaw/c_bind_riemannsolvers.f90:4-6), then the Lax-Friedrichs family of
+ * compute_lf_flux (src/SWE/SWE_euler_timestep.f90:359-446). The reference picks
+ * one at compile time (SConstruct:223-237); here it is a runtime parameter. */
+#define SWE_SOLVER_FWAVE 1
+#define SWE_SOLVER_AUG_RIEMANN 3
+#define SWE_SOLVER_LF 10
+#define SWE_SOLVER_LF_BATH 11
+#define SWE_SOLVER_LLF 12
+#define SWE_SOLVER_LLF_BATH 13
+
+/* domain-boundary conditions of bnd_skeleton_scalar_op
+ * (src/SWE/SWE_euler_timestep.f90:241-248): OUTFLOW is the active one in the
+ * reference; SLIP and NOSLIP are its commented-out alternatives. */
+#define SWE_BC_OUTFLOW 0
+#define SWE_BC_SLIP 1
+#define SWE_BC_NOSLIP 2
+
+/* Runtime parameters the step reads from cfg (src/Config.f90:30-121). */
+typedef struct swe_params {
+    int32_t solver;            /* SWE_SOLVER_* */
+    int32_t bc;                /* SWE_BC_* */
+    double dry_tolerance;      /* cfg%dry_tolerance [m] */
+    double courant;            /* cfg%courant_number */
+    double scaling;            /* cfg%scaling: domain edge length */
+    int32_t min_depth;         /* cfg%i_min_depth */
+    int32_t max_depth;         /* cfg%i_max_depth */
+    double max_time;           /* cfg%r_max_time, <= 0 disables the dt clamp */
+    double output_time_step;   /* cfg%r_output_time_step, <= 0 disables the dt clamp */
+} swe_params;
+
+typedef struct swe_ctx swe_ctx;
+
+/* Create a context on CUDA device `device`. Replaces the creation of the
+ * euler traversal in t_swe%create (src/SWE/SWE.f90:52-88). */
+int swe_create(swe_ctx** ctx, int device);
+
+/* Free all device memory of the context. Replaces swe_destroy (src/SWE/SWE.f90:173-203). */
+int swe_destroy(swe_ctx* ctx);
+
+/* Launch work on this stream (a cudaStream_t, NULL = the context's own stream). */
+int swe_set_stream(swe_ctx* ctx, void* stream);
+
+/* Set the runtime parameters (the cfg fields of src/Config.f90:30-121 and the
+ * compile-time flux choice of SConstruct:223-237). */
+int swe_set_params(swe_ctx* ctx, const swe_params* params);
+
+/* Upload a mesh after a remesh. Replaces the cell and edge streams the
+ * traversal reads (t_grid_section, src/Tools_grid.f90:480-515); the layout
+ * follows the index maps of samoa_get_grid (src/Generic/samoa.h:25-57).
+ *   depth[n_cells], plotter[n_cells]   cell depth and plotter-grammar type (+-1..+-8)
+ *   edge_cells[2*n_edges]              the two cells of each inner edge
+ *   edge_local[2*n_edges]              the edge's local index (1..3) in each cell
+ *   bnd_cell[n_bnd], bnd_local[n_bnd]  domain-boundary edges
+ * Every (cell, local index) must be used exactly once. Invalidates the state. */
+int swe_mesh_upload(swe_ctx* ctx, int64_t n_cells, const int8_t* depth, const int8_t* plotter,
+                    int64_t n_edges, const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd,
+                    const int64_t* bnd_cell, const int8_t* bnd_local);
+
+/* Copy the cell state in/out (host pointers, n_cells doubles each; b is read-only
+ * for the step). Replaces gv_Q%read/write on the cells' data_pers%Q
+ * (src/Tools_grid_variable.f90:146-193). Download synchronises. */
+int swe_state_upload(swe_ctx* ctx, const double* h, const double* hu, const double* hv, const double* b);
+int swe_state_download(swe_ctx* ctx, double* h, double* hu, double* hv, double* b);
+
+/* Device pointers of the current state (valid until the next step or upload). */
+int swe_state_device(swe_ctx* ctx, double** h, double** hu, double** hv, const double** b);
+
+/* grid%r_time and grid%r_dt (src/SWE/SWE_data_types.f90:126-130). The step
+ * uses dt (clamped by max_time / output_time_step) and leaves
+ * dt = courant * min_cells(volume / sum(len * max_wave_speed)) for the next
+ * step (src/SWE/SWE_euler_timestep.f90:89-131). swe_get_time synchronises. */
+int swe_set_time(swe_ctx* ctx, double time, double dt);
+int swe_get_time(swe_ctx* ctx, double* time, double* dt, double* dt_new);
+
+/* Run n_steps time steps, asynchronously on the context's stream.
+ * Replaces n_steps calls of swe%euler%traverse(grid) (src/SWE/SWE.f90:393). */
+int swe_traverse(swe_ctx* ctx, int64_t n_steps);
+
+/* Refinement flags of the last step (-1 coarsen, 0 keep, 1 refine; int8 per
+ * cell in upload order) and the number of refinements it issued
+ * (src/SWE/SWE_euler_timestep.f90:117,336-344). Synchronises. */
+int swe_get_refinements(swe_ctx* ctx, int8_t* flags, int64_t* n_refinements);
+
+/* Number of steps run since the last mesh upload (its parity is the current
+ * traversal direction: odd = reversed). Synchronises. */
+int swe_get_step_count(swe_ctx* ctx, int64_t* steps);
+
+/* Block until all work of the context has finished; reports device errors. */
+int swe_synchronize(swe_ctx* ctx);
+
+/* Message of the last failure on this thread (always NUL-terminated). */
+int swe_last_error(char* buf, size_t n);
+
+/* Kernel tuning: cells per segment (even, 64..2048) and threads per block
+ * (multiple of 32, 64..1024); 0 keeps the current value. A mesh upload or
+ * this call rebuilds the segment task lists. */
+int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
+int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads);
+
+/* Uniform Sierpinski mesh of the unit square at reference depth `depth`
+ * (2^(depth+1) cells) in traversal order, restating init_grid
+ * (src/SFC_node_traversal.f90:22-145). Call with NULL outputs to get the sizes.
+ * Inner edges are numbered in first-touch order (colour edge before next
+ * edge, src/Tools_adaptive_traversal.f90:585-603), boundary edges in walk order.
+ * centroids (optional, may be NULL): 2 doubles per cell, the mean of the
+ * three corners in the unit square. */
+int swe_mesh_uniform(int32_t depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
+                     int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell,
+                     int8_t* bnd_local, double* centroids);
+
+/* Check a mesh in the swe_mesh_upload layout on the host without a context
+ * (same checks as the upload): 0 if valid, SWE_E_INVALID with a message otherwise. */
+int swe_mesh_validate(int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
+                      const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
+                      const int8_t* bnd_local);
+
+/* Evaluate the edge flux of one solver on n independent edges on the device:
+ * the skeleton operator of src/SWE/SWE_euler_timestep.f90:196-215 with
+ * compute_geoclaw_flux / compute_lf_flux. Host arrays: normals[2n],
+ * q_left[4n], q_right[4n] as (h, hu, hv, b); out_left[4n], out_right[4n] as
+ * (h, hu, hv, max_wave_speed) net updates. For solver-level checks. */
+int swe_riemann_batch(int32_t solver, int64_t n, const double* normals, const double* q_left, const double* q_right,
+                      double dry_tolerance, double* out_left, double* out_right);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SAMOA_SWE_H */

@@ -1,0 +1,66 @@
+// Internal declarations shared by the host and device parts of the SWE step library.
+#pragma once
+
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/samoa_swe.h"
+
+namespace swe {
+
+constexpr int kMaxDepth = 60;  // bit_size(int64) - 4, src/SFC_data_types.f90:77
+
+// One edge task of a segment: 16 bytes, loaded with one 128-bit load.
+//   a, b: cells (b = -1 for a domain-boundary edge); on an inner edge a < b.
+//   meta: bits 0-1 local edge index of a (0..2), bits 2-3 of b,
+//         bits 4-8 plotter type of a + 8, bits 9-13 of b + 8, bit 14 boundary.
+struct alignas(16) Task {
+    int32_t a, b;
+    uint32_t meta;
+    uint32_t pad;
+};
+
+inline uint32_t pack_meta(int la, int lb, int pa, int pb, bool bnd) {
+    return (uint32_t)la | ((uint32_t)lb << 2) | ((uint32_t)(pa + 8) << 4) | ((uint32_t)(pb + 8) << 9) |
+           ((uint32_t)(bnd ? 1 : 0) << 14);
+}
+
+// Device-resident scalars of a context. The step kernel reads step and dt,
+// reduces into dt_acc / refine_acc, and the last block to finish advances time,
+// dt and step, so many steps run back to back without the host.
+struct DevScalars {
+    double time;                    // grid%r_time
+    double dt;                      // grid%r_dt for the next step
+    double dt_new;                  // min(volume / sum(len * speed)) of the last step
+    unsigned long long dt_acc;      // bits of the running minimum (non-negative doubles order as integers)
+    unsigned long long refine_acc;  // refinements issued in the running step
+    unsigned long long n_refine;    // refinements issued in the last step
+    unsigned int done;              // blocks finished in the running step
+    unsigned int error;             // nonzero: a kernel saw a bad index or a wait ran out
+    long long step;                 // steps since the mesh upload (parity = traversal direction)
+};
+
+// Mesh as ingested from the C ABI (validated, a < b on inner edges).
+struct HostMesh {
+    int64_t n_cells = 0, n_edges = 0, n_bnd = 0;
+    int min_depth = 0, max_depth = 0;
+    std::vector<int8_t> depth, plotter;
+    std::vector<int64_t> ea, eb, bc;
+    std::vector<int8_t> la, lb, bl;
+};
+
+int set_error(int code, const char* fmt, ...);
+
+int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
+                 int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell,
+                 int8_t* bnd_local, double* centroids);
+int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
+                const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
+                const int8_t* bnd_local);
+int build_tasks(const HostMesh& m, int32_t seg_cells, std::vector<int64_t>& seg_ptr, std::vector<Task>& tasks);
+
+// Geometry tables restating src/SFC_data_types.f90:509-700 (host side, exact).
+void geometry_tables(double leg[kMaxDepth + 2], double vol[kMaxDepth + 1], double normal[17][3][2]);
+
+}  // namespace swe

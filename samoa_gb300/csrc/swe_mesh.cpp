@@ -1,0 +1,283 @@
+// Host side of the mesh: the uniform Sierpinski mesh generator (a restatement of
+// init_grid, src/SFC_node_traversal.f90:22-292) and the conversion of a mesh
+// in the C-ABI layout into the per-segment edge task lists the step kernel
+// reads. Both run once per remesh, not per step.
+#include "swe_internal.h"
+
+#include <cstring>
+#include <vector>
+
+namespace swe {
+
+namespace {
+
+// Sierpinski grammar state of one cell (src/SFC_data_types.f90:84-91).
+struct GrammarCell {
+    int8_t prev_bnd, next_bnd;  // previous / next crossed edge on the domain boundary
+    int8_t color_type;          // OLD = 0, NEW = 1, OLD_BND = 2, NEW_BND = 3
+    int8_t depth, plotter, turtle, color;
+};
+
+constexpr int kK = 1, kV = 2, kH = 3;
+constexpr int kRed = -1, kGreen = 0;
+
+// Children of a bisected cell, create_child_cells (src/SFC_node_traversal.f90:252-292).
+void bisect(const GrammarCell& p, GrammarCell& c1, GrammarCell& c2) {
+    static const int8_t first_turtle[4] = {0, kH, kH, kV};
+    static const int8_t second_turtle[4] = {0, kV, kK, kK};
+    // i_plotter_child_type(-8:8)
+    static const int8_t child_plotter[17] = {3, 2, 1, 8, 7, 6, 5, 4, 0, -6, -7, -8, -1, -2, -3, -4, -5};
+    c1.turtle = first_turtle[p.turtle];
+    c2.turtle = second_turtle[p.turtle];
+    c1.plotter = child_plotter[p.plotter + 8];
+    c2.plotter = (int8_t)-child_plotter[-p.plotter + 8];
+    c1.depth = c2.depth = (int8_t)(p.depth + 1);
+    const int8_t flip = (int8_t)(kRed + kGreen - p.color);
+    // first child: previous edge of the parent, new crossed edge to the sibling
+    c1.prev_bnd = p.prev_bnd;
+    c1.next_bnd = 0;
+    // second child: old crossed edge from the sibling, next edge of the parent
+    c2.prev_bnd = 0;
+    c2.next_bnd = p.next_bnd;
+    if (p.turtle == kK) {
+        c1.color_type = (int8_t)(1 | (p.next_bnd << 1));  // the parent's next edge
+        c2.color_type = p.color_type;
+        c1.color = flip;
+        c2.color = p.color;
+    } else if (p.turtle == kV) {
+        c1.color_type = p.color_type;
+        c2.color_type = p.color_type;
+        c1.color = c2.color = p.color;
+    } else {
+        c1.color_type = p.color_type;
+        c2.color_type = (int8_t)(0 | (p.prev_bnd << 1));  // the parent's previous edge
+        c1.color = p.color;
+        c2.color = flip;
+    }
+}
+
+// Local edge index (1..3) of the previous, colour and next edge per turtle type
+// (cell_get_edge_indices, src/SFC_data_types.f90:370-384).
+const int8_t kPrevIdx[4] = {0, 3, 3, 2};
+const int8_t kColorIdx[4] = {0, 1, 2, 3};
+const int8_t kNextIdx[4] = {0, 2, 1, 1};
+
+}  // namespace
+
+int64_t uniform_boundary_edges(int depth) { return (int64_t)4 << (depth / 2); }
+
+int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
+                 int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell, int8_t* bnd_local,
+                 double* centroids) {
+    if (depth < 0 || depth > 29) return set_error(SWE_E_INVALID, "mesh depth %d out of range 0..29", depth);
+    const int64_t n = (int64_t)2 << depth;
+    const int64_t nb = uniform_boundary_edges(depth);
+    const int64_t ne = (3 * n - nb) / 2;
+    if (n_cells) *n_cells = n;
+    if (n_edges) *n_edges = ne;
+    if (n_bnd) *n_bnd = nb;
+    if (!depth_out && !plotter_out && !edge_cells && !edge_local && !bnd_cell && !bnd_local && !centroids)
+        return SWE_OK;
+    if (!depth_out || !plotter_out || !edge_cells || !edge_local || !bnd_cell || !bnd_local)
+        return set_error(SWE_E_INVALID, "mesh outputs must all be given (centroids optional)");
+
+    // Depth-first bisection with an explicit stack; leaves come out in curve order.
+    struct Item {
+        GrammarCell c;
+        double x[3][2];
+    };
+    std::vector<Item> stack;
+    stack.reserve(2 * (size_t)depth + 8);
+    // the two root triangles of the unit square (init_section, src/SFC_node_traversal.f90:90-109);
+    // pushed in reverse so the first one is expanded first
+    Item r2{{0, 1, 3, 0, -6, kH, kRed}, {{1, 1}, {0, 1}, {0, 0}}};
+    Item r1{{1, 0, 2, 0, -2, kK, kRed}, {{0, 0}, {1, 0}, {1, 1}}};
+    stack.push_back(r2);
+    stack.push_back(r1);
+
+    std::vector<int64_t> color_stack[2];
+    int64_t open_crossed = -1, next_edge = 0, next_bnd = 0, k = 0;
+    while (!stack.empty()) {
+        Item it = stack.back();
+        stack.pop_back();
+        if (it.c.depth < depth) {
+            Item a, b;
+            bisect(it.c, a.c, b.c);
+            double mx = 0.5 * (it.x[0][0] + it.x[2][0]), my = 0.5 * (it.x[0][1] + it.x[2][1]);
+            a.x[0][0] = it.x[0][0]; a.x[0][1] = it.x[0][1];
+            a.x[1][0] = mx; a.x[1][1] = my;
+            a.x[2][0] = it.x[1][0]; a.x[2][1] = it.x[1][1];
+            b.x[0][0] = it.x[1][0]; b.x[0][1] = it.x[1][1];
+            b.x[1][0] = mx; b.x[1][1] = my;
+            b.x[2][0] = it.x[2][0]; b.x[2][1] = it.x[2][1];
+            stack.push_back(b);
+            stack.push_back(a);
+            continue;
+        }
+        // a leaf: cell number k in traversal order
+        const GrammarCell& c = it.c;
+        depth_out[k] = c.depth;
+        plotter_out[k] = c.plotter;
+        if (centroids) {
+            centroids[2 * k] = ((it.x[0][0] + it.x[1][0]) + it.x[2][0]) / 3.0;
+            centroids[2 * k + 1] = ((it.x[0][1] + it.x[1][1]) + it.x[2][1]) / 3.0;
+        }
+        const int8_t ip = kPrevIdx[c.turtle], ic = kColorIdx[c.turtle], in = kNextIdx[c.turtle];
+        // previous crossed edge: the open crossed edge of the previous cell, or the boundary
+        if (!c.prev_bnd) {
+            if (open_crossed < 0) return set_error(SWE_E_INVALID, "mesh walk: missing crossed edge");
+            edge_cells[2 * open_crossed + 1] = k;
+            edge_local[2 * open_crossed + 1] = ip;
+        } else {
+            bnd_cell[next_bnd] = k;
+            bnd_local[next_bnd++] = ip;
+        }
+        open_crossed = -1;
+        // colour edge: first touch pushes, second touch pops
+        std::vector<int64_t>& cs = color_stack[c.color + 1];
+        if (c.color_type == 0) {
+            if (cs.empty()) return set_error(SWE_E_INVALID, "mesh walk: colour stack underflow");
+            int64_t e = cs.back();
+            cs.pop_back();
+            edge_cells[2 * e + 1] = k;
+            edge_local[2 * e + 1] = ic;
+        } else if (c.color_type == 1) {
+            int64_t e = next_edge++;
+            cs.push_back(e);
+            edge_cells[2 * e] = k;
+            edge_local[2 * e] = ic;
+        } else {
+            bnd_cell[next_bnd] = k;
+            bnd_local[next_bnd++] = ic;
+        }
+        // next crossed edge
+        if (!c.next_bnd) {
+            int64_t e = next_edge++;
+            edge_cells[2 * e] = k;
+            edge_local[2 * e] = in;
+            open_crossed = e;
+        } else {
+            bnd_cell[next_bnd] = k;
+            bnd_local[next_bnd++] = in;
+        }
+        ++k;
+    }
+    if (k != n || next_edge != ne || next_bnd != nb || open_crossed >= 0 || !color_stack[0].empty() ||
+        !color_stack[1].empty())
+        return set_error(SWE_E_INVALID, "mesh walk inconsistent");
+    return SWE_OK;
+}
+
+// Per-segment edge tasks. An inner edge with both cells in one segment is one
+// task there; an edge between two segments is a task in both (each keeps its
+// own side, so no segment waits for another). A boundary edge is a task in its
+// cell's segment.
+int build_tasks(const HostMesh& m, int32_t T, std::vector<int64_t>& seg_ptr, std::vector<Task>& tasks) {
+    const int64_t n = m.n_cells;
+    const int64_t nseg = (n + T - 1) / T;
+    seg_ptr.assign((size_t)nseg + 1, 0);
+    for (int64_t e = 0; e < m.n_edges; ++e) {
+        int64_t sa = m.ea[e] / T, sb = m.eb[e] / T;
+        seg_ptr[sa + 1]++;
+        if (sb != sa) seg_ptr[sb + 1]++;
+    }
+    for (int64_t j = 0; j < m.n_bnd; ++j) seg_ptr[m.bc[j] / T + 1]++;
+    for (int64_t s = 0; s < nseg; ++s) seg_ptr[s + 1] += seg_ptr[s];
+    tasks.resize((size_t)seg_ptr[nseg]);
+    std::vector<int64_t> fill(seg_ptr.begin(), seg_ptr.end() - 1);
+    // boundary edges first inside each segment, then inner edges in stream order
+    for (int64_t j = 0; j < m.n_bnd; ++j) {
+        int64_t c = m.bc[j];
+        Task t;
+        t.a = (int32_t)c;
+        t.b = -1;
+        t.meta = pack_meta(m.bl[j] - 1, 0, m.plotter[c], 1, true);
+        t.pad = 0;
+        tasks[(size_t)fill[c / T]++] = t;
+    }
+    for (int64_t e = 0; e < m.n_edges; ++e) {
+        int64_t a = m.ea[e], b = m.eb[e];
+        Task t;
+        t.a = (int32_t)a;
+        t.b = (int32_t)b;
+        t.meta = pack_meta(m.la[e] - 1, m.lb[e] - 1, m.plotter[a], m.plotter[b], false);
+        t.pad = 0;
+        int64_t sa = a / T, sb = b / T;
+        tasks[(size_t)fill[sa]++] = t;
+        if (sb != sa) tasks[(size_t)fill[sb]++] = t;
+    }
+    return SWE_OK;
+}
+
+// Validate a mesh given through the C ABI and store it with a < b per edge.
+int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
+                const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
+                const int8_t* bnd_local) {
+    if (n_cells <= 0 || n_cells >= ((int64_t)1 << 31) - 1)
+        return set_error(SWE_E_INVALID, "n_cells %lld out of range", (long long)n_cells);
+    if (n_edges < 0 || n_bnd < 0 || 2 * n_edges + n_bnd != 3 * n_cells)
+        return set_error(SWE_E_INVALID, "edge counts inconsistent: 2*%lld + %lld != 3*%lld", (long long)n_edges,
+                         (long long)n_bnd, (long long)n_cells);
+    if (!depth || !plotter || (n_edges && (!edge_cells || !edge_local)) || (n_bnd && (!bnd_cell || !bnd_local)))
+        return set_error(SWE_E_INVALID, "null mesh array");
+    m.n_cells = n_cells;
+    m.n_edges = n_edges;
+    m.n_bnd = n_bnd;
+    m.depth.assign(depth, depth + n_cells);
+    m.plotter.assign(plotter, plotter + n_cells);
+    int dmin = 127, dmax = -1;
+    for (int64_t c = 0; c < n_cells; ++c) {
+        int d = depth[c], p = plotter[c];
+        if (d < 0 || d > kMaxDepth) return set_error(SWE_E_INVALID, "cell %lld: depth %d", (long long)c, d);
+        if (p == 0 || p < -8 || p > 8) return set_error(SWE_E_INVALID, "cell %lld: plotter type %d", (long long)c, p);
+        if (d < dmin) dmin = d;
+        if (d > dmax) dmax = d;
+    }
+    m.min_depth = dmin;
+    m.max_depth = dmax;
+    std::vector<uint8_t> used((size_t)n_cells, 0);
+    auto claim = [&](int64_t c, int l) -> bool {
+        uint8_t bit = (uint8_t)(1u << (l - 1));
+        if (used[(size_t)c] & bit) return false;
+        used[(size_t)c] |= bit;
+        return true;
+    };
+    m.ea.resize((size_t)n_edges);
+    m.eb.resize((size_t)n_edges);
+    m.la.resize((size_t)n_edges);
+    m.lb.resize((size_t)n_edges);
+    for (int64_t e = 0; e < n_edges; ++e) {
+        int64_t a = edge_cells[2 * e], b = edge_cells[2 * e + 1];
+        int la = edge_local[2 * e], lb = edge_local[2 * e + 1];
+        if (a < 0 || a >= n_cells || b < 0 || b >= n_cells || a == b)
+            return set_error(SWE_E_INVALID, "edge %lld: cells (%lld, %lld) invalid", (long long)e, (long long)a,
+                             (long long)b);
+        if (la < 1 || la > 3 || lb < 1 || lb > 3)
+            return set_error(SWE_E_INVALID, "edge %lld: local index out of 1..3", (long long)e);
+        if (!claim(a, la) || !claim(b, lb))
+            return set_error(SWE_E_INVALID, "edge %lld: a cell's local edge is used twice", (long long)e);
+        if (b < a) {
+            std::swap(a, b);
+            std::swap(la, lb);
+        }
+        m.ea[(size_t)e] = a;
+        m.eb[(size_t)e] = b;
+        m.la[(size_t)e] = (int8_t)la;
+        m.lb[(size_t)e] = (int8_t)lb;
+    }
+    m.bc.resize((size_t)n_bnd);
+    m.bl.resize((size_t)n_bnd);
+    for (int64_t j = 0; j < n_bnd; ++j) {
+        int64_t c = bnd_cell[j];
+        int l = bnd_local[j];
+        if (c < 0 || c >= n_cells || l < 1 || l > 3)
+            return set_error(SWE_E_INVALID, "boundary edge %lld invalid", (long long)j);
+        if (!claim(c, l)) return set_error(SWE_E_INVALID, "boundary edge %lld: local edge used twice", (long long)j);
+        m.bc[(size_t)j] = c;
+        m.bl[(size_t)j] = (int8_t)l;
+    }
+    // 2*n_edges + n_bnd == 3*n_cells and no slot claimed twice => every slot used once
+    return SWE_OK;
+}
+
+}  // namespace swe

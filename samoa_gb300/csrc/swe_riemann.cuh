@@ -1,0 +1,385 @@
+// Device-side edge fluxes of the SWE step: the GeoClaw double-precision Riemann
+// solvers and the Lax-Friedrichs fluxes, evaluated per edge in FP64.
+//
+// Bit-for-bit agreement with the CPU restatement needs the same rounding at
+// every operation: this file is compiled with --fmad=false (no contraction)
+// and keeps the reference's left-to-right evaluation order of each expression.
+// Sums written in the reference as dot_product/matmul start from +0.0; that
+// first addition only turns a -0.0 into +0.0, which z0() does with integer
+// instructions instead of spending an FP64 add.
+#pragma once
+
+#include <stdint.h>
+
+namespace swe {
+
+constexpr double kG = 9.80665;  // src/SWE/SWE_data_types.f90:34
+
+enum Solver : int { FWAVE = 1, AUG_RIEMANN = 3, LF = 10, LF_BATH = 11, LLF = 12, LLF_BATH = 13 };
+enum Boundary : int { BC_OUTFLOW = 0, BC_SLIP = 1, BC_NOSLIP = 2 };
+
+struct State {
+    double h, p1, p2, b;  // surface elevation, momentum, bathymetry
+};
+struct Update {
+    double h, p1, p2, s;  // net update (or flux) and maximum wave speed
+};
+
+__device__ __forceinline__ double z0(double x) {
+    long long v = __double_as_longlong(x);
+    return __longlong_as_double(v == (long long)0x8000000000000000ULL ? 0LL : v);
+}
+__device__ __forceinline__ double dmn(double a, double b) { return (a < b) ? a : b; }
+__device__ __forceinline__ double dmx(double a, double b) { return (a > b) ? a : b; }
+
+// Riemann structure with one Newton step, src/geoclaw/riemannsolvers.f:507-618.
+__device__ __noinline__ void riemann_structure(double hL, double hR, double uL, double uR, double drytol,
+                                               double& hm, double& s1m, double& s2m) {
+    const double g = kG;
+    double h_min = dmn(hR, hL);
+    double h_max = dmx(hR, hL);
+    double delu = uR - uL;
+    if (h_min <= drytol) {
+        hm = 0.0;
+        double t = ((uR + uL) - 2.0 * sqrt(g * hR)) + 2.0 * sqrt(g * hL);
+        s1m = t;
+        s2m = t;
+        return;
+    }
+    double F_min = delu + 2.0 * (sqrt(g * h_min) - sqrt(g * h_max));
+    double F_max = delu + (h_max - h_min) * sqrt(((0.5 * g) * (h_max + h_min)) / (h_max * h_min));
+    if (F_min > 0.0) {  // two rarefactions
+        double t = dmx(0.0, -delu + 2.0 * (sqrt(g * hL) + sqrt(g * hR)));
+        hm = (1.0 / (16.0 * g)) * (t * t);
+        s1m = (uL + 2.0 * sqrt(g * hL)) - 3.0 * sqrt(g * hm);
+        s2m = (uR - 2.0 * sqrt(g * hR)) + 3.0 * sqrt(g * hm);
+    } else if (F_max <= 0.0) {  // two shocks: one Newton step on sqrt(h)
+        double h0 = h_max;
+        double gL = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hL));
+        double gR = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hR));
+        double F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR;
+        double dfdh = ((gL - (g * (h0 - hL)) / ((4.0 * (h0 * h0)) * gL)) + gR) -
+                      (g * (h0 - hR)) / ((4.0 * (h0 * h0)) * gR);
+        double slope = (2.0 * sqrt(h0)) * dfdh;
+        double t = sqrt(h0) - F0 / slope;
+        hm = t * t;
+        double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hL));
+        double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hR));
+        s1m = u1m - sqrt(g * hm);
+        s2m = u2m + sqrt(g * hm);
+    } else {  // one shock, one rarefaction
+        double h0 = h_min;
+        double F0 = (delu + 2.0 * (sqrt(g * h0) - sqrt(g * h_max))) +
+                    (h0 - h_min) * sqrt((0.5 * g) * (1.0 / h0 + 1.0 / h_min));
+        double slope = (F_max - F0) / (h_max - h_min);
+        hm = h0 - F0 / slope;
+        if (hL > hR) {
+            s1m = (uL + 2.0 * sqrt(g * hL)) - 3.0 * sqrt(g * hm);
+            s2m = (uL + 2.0 * sqrt(g * hL)) - sqrt(g * hm);
+        } else {
+            s2m = (uR - 2.0 * sqrt(g * hR)) + 3.0 * sqrt(g * hm);
+            s1m = (uR - 2.0 * sqrt(g * hR)) + sqrt(g * hm);
+        }
+    }
+}
+
+__device__ __forceinline__ double det3(double a00, double a01, double a02, double a10, double a11, double a12,
+                                       double a20, double a21, double a22) {
+    double d1 = a00 * (a11 * a22 - a12 * a21);
+    double d2 = a01 * (a10 * a22 - a12 * a20);
+    double d3 = a02 * (a10 * a21 - a11 * a20);
+    return (d1 - d2) + d3;
+}
+
+// Augmented solver (George 2008) with maxiter = 1, src/geoclaw/riemannsolvers.f:2-258.
+// The entropy corrector is off in the source; with one iteration the star
+// states after the Cramer solve never reach the outputs.
+__device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
+                                         double uL, double uR, double vL, double vR, double delphi, double sE1,
+                                         double sE2, double drytol, double sw[3], double fw[3][3]) {
+    const double g = kG;
+    double delh = hR - hL;
+    double delhu = huR - huL;
+    double delb = bR - bL;
+    double hm, s1m, s2m;
+    riemann_structure(hL, hR, uL, uR, drytol, hm, s1m, s2m);
+    double l0 = dmn(sE1, s2m);
+    double l2 = dmx(sE2, s1m);
+    sE1 = l0;
+    sE2 = l2;
+    double hstarHLL = dmx((((huL - huR) + sE2 * hR) - sE1 * hL) / (sE2 - sE1), 0.0);
+    double l1 = 0.5 * (l0 + l2);
+    if (fabs(l1) < 1e-20) l1 = 0.0;
+    // eigenvectors: columns (1, l, l^2) for waves 1 and 3, (0, 0, 1) for wave 2
+    const double r00 = 1.0, r01 = 0.0, r02 = 1.0;
+    const double r10 = l0, r11 = 0.0, r12 = l2;
+    const double r20 = l0 * l0, r21 = 1.0, r22 = l2 * l2;
+
+    const double ct = 1e-6;
+    double hbar = dmx(0.5 * (hL + hR), 0.0);
+    double su = uL + uR;
+    double s1s2bar = 0.25 * (su * su) - g * hbar;
+    double s1s2tilde = dmx(0.0, uL * uR) - g * hbar;
+    bool sonic = false;
+    if (fabs(s1s2bar) <= ct) sonic = true;
+    if (s1s2bar * s1s2tilde <= ct) sonic = true;
+    if ((s1s2bar * sE1) * sE2 <= ct) sonic = true;
+    if (dmn(fabs(sE1), fabs(sE2)) < ct) sonic = true;
+    if (sE1 < 0.0 && s1m > 0.0) sonic = true;
+    if (sE2 > 0.0 && s2m < 0.0) sonic = true;
+    if ((uL + sqrt(g * hL)) * (uR + sqrt(g * hR)) < 0.0) sonic = true;
+    if ((uL - sqrt(g * hL)) * (uR - sqrt(g * hR)) < 0.0) sonic = true;
+
+    double deldelh = sonic ? -delb : ((delb * g) * hbar) / s1s2bar;
+    if (sE1 < -ct && sE2 > ct) {
+        deldelh = dmn(deldelh, (hstarHLL * (sE2 - sE1)) / sE2);
+        deldelh = dmx(deldelh, (hstarHLL * (sE2 - sE1)) / sE1);
+    } else if (sE1 >= ct) {
+        deldelh = dmn(deldelh, (hstarHLL * (sE2 - sE1)) / sE1);
+        deldelh = dmx(deldelh, -hL);
+    } else if (sE2 <= -ct) {
+        deldelh = dmn(deldelh, hR);
+        deldelh = dmx(deldelh, (hstarHLL * (sE2 - sE1)) / sE2);
+    }
+    double deldelphi = sonic ? -((g * hbar) * delb) : -((((delb * g) * hbar) * s1s2tilde) / s1s2bar);
+    deldelphi = dmn(deldelphi, g * dmx(-(hL * delb), -(hR * delb)));
+    deldelphi = dmx(deldelphi, g * dmn(-(hL * delb), -(hR * delb)));
+    double d0 = delh - deldelh, d1 = delhu, d2 = delphi - deldelphi;
+
+    double det = det3(r00, r01, r02, r10, r11, r12, r20, r21, r22);
+    double beta0 = det3(d0, r01, r02, d1, r11, r12, d2, r21, r22) / det;
+    double beta1 = det3(r00, d0, r02, r10, d1, r12, r20, d2, r22) / det;
+    double beta2 = det3(r00, r01, d0, r10, r11, d1, r20, r21, d2) / det;
+
+    sw[0] = l0;
+    sw[1] = l1;
+    sw[2] = l2;
+    fw[0][0] = beta0 * r10; fw[1][0] = beta0 * r20; fw[2][0] = beta0 * r10;
+    fw[0][1] = beta1 * r11; fw[1][1] = beta1 * r21; fw[2][1] = beta1 * r11;
+    fw[0][2] = beta2 * r12; fw[1][2] = beta2 * r22; fw[2][2] = beta2 * r12;
+    fw[2][0] = fw[2][0] * vL;
+    fw[2][2] = fw[2][2] * vR;
+    fw[2][1] = ((((hR * uR) * vR) - ((hL * uL) * vL)) - fw[2][0]) - fw[2][2];
+}
+
+// Wet/dry handling, wave speeds and net updates of c_bind_geoclaw_solver_dp
+// (src/geoclaw/c_bind_riemannsolvers.f90:16-176) with the f-wave
+// (src/geoclaw/riemannsolvers.f:446-500) or augmented solver. netL/netR are
+// the left/right net updates of (h, hu, hv) in the edge frame.
+template <int SOLVER>
+__device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL, double huR, double hvL,
+                                               double hvR, double bL, double bR, double drytol, double netL[3],
+                                               double netR[3], double& maxspeed) {
+    const double g = kG;
+    netL[0] = netL[1] = netL[2] = 0.0;
+    netR[0] = netR[1] = netR[2] = 0.0;
+    maxspeed = 0.0;
+    if (hL <= drytol && hR <= drytol) return;
+    double uL, uR, vL, vR;
+    if (hR > drytol) {
+        uR = huR / hR;
+        vR = hvR / hR;
+    } else {
+        hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0;
+    }
+    if (hL > drytol) {
+        uL = huL / hL;
+        vL = hvL / hL;
+    } else {
+        hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0;
+    }
+    bool wall_l = false, wall_r = false;  // wall(1) = 0 resp. wall(3) = 0 (wall(2) = 0 with either)
+    if (hR <= drytol) {
+        double hstar, s1m, s2m;
+        riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);
+        double hstartest = dmx(hL, hstar);
+        if (hstartest + bL < bR) {
+            wall_r = true;
+            hR = hL; huR = -huL; bR = bL; uR = -uL; vR = vL;
+        } else if (hL + bL < bR) {
+            bR = hL + bL;
+        }
+    } else if (hL <= drytol) {
+        double hstar, s1m, s2m;
+        riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);
+        double hstartest = dmx(hR, hstar);
+        if (hstartest + bR < bL) {
+            wall_l = true;
+            hL = hR; huL = -huR; bL = bR; uL = -uR; vL = vR;
+        } else if (hR + bR < bL) {
+            bL = hR + bR;
+        }
+    }
+    double delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) +
+                     (((0.5 * g) * (((bR + hR) - bL) - hL)) * (hR + hL))) -
+                    (((0.5 * g) * (hR + hL)) * (bR - bL));
+    double sqL = sqrt(g * hL), sqR = sqrt(g * hR);
+    double sL = uL - sqL;
+    double sR = uR + sqR;
+    double uhat = (sqL * uL + sqR * uR) / (sqR + sqL);
+    double chat = sqrt((g * 0.5) * (hR + hL));
+    double sE1 = dmn(sL, uhat - chat);
+    double sE2 = dmx(sR, uhat + chat);
+
+    double sw[3], fw[3][3];
+    if (SOLVER == AUG_RIEMANN) {
+        riemann_aug(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, drytol, sw, fw);
+    } else {
+        double delhu = huR - huL;
+        double delb = bR - bL;
+        double deldelphi = -(((g * 0.5) * (hR + hL)) * delb);
+        double dpd = delphi - deldelphi;
+        double beta1 = (sE2 * delhu - dpd) / (sE2 - sE1);
+        double beta2 = (dpd - sE1 * delhu) / (sE2 - sE1);
+        sw[0] = sE1; sw[1] = 0.5 * (sE1 + sE2); sw[2] = sE2;
+        fw[0][0] = beta1; fw[1][0] = beta1 * sE1; fw[2][0] = beta1 * vL;
+        fw[0][2] = beta2; fw[1][2] = beta2 * sE2; fw[2][2] = beta2 * vR;
+        fw[0][1] = 0.0; fw[1][1] = 0.0;
+        fw[2][1] = ((huR * vR - huL * vL) - fw[2][0]) - fw[2][2];
+    }
+    // eliminate ghost fluxes of a wall (multiplication by 0 keeps the sign of zero)
+    if (wall_l || wall_r) {
+        int w0 = wall_l ? 0 : 1;
+        for (int w = w0; w < w0 + 2; ++w) {
+            sw[w] = sw[w] * 0.0;
+            fw[0][w] = fw[0][w] * 0.0;
+            fw[1][w] = fw[1][w] * 0.0;
+            fw[2][w] = fw[2][w] * 0.0;
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+#pragma unroll
+        for (int w = 0; w < 3; ++w) {
+            if (sw[w] < 0.0) {
+                netL[e] = netL[e] + fw[e][w];
+            } else if (sw[w] > 0.0) {
+                netR[e] = netR[e] + fw[e][w];
+            } else {
+                netL[e] = netL[e] + 0.5 * fw[e][w];
+                netR[e] = netR[e] + 0.5 * fw[e][w];
+            }
+        }
+    }
+    double m = fabs(sw[0]);
+    if (fabs(sw[1]) > m) m = fabs(sw[1]);
+    if (fabs(sw[2]) > m) m = fabs(sw[2]);
+    maxspeed = m;
+}
+
+// compute_geoclaw_flux, src/SWE/SWE_euler_timestep.f90:449-481
+template <int SOLVER>
+__device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR,
+                                             double drytol, Update& fL, Update& fR) {
+    // T = [[n1, n2], [-n2, n1]]; p_edge = T p
+    double pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
+    double pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
+    double pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
+    double pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+    double netL[3], netR[3], ms;
+    geoclaw_solver<SOLVER>(QL.h - QL.b, QR.h - QR.b, pL1, pR1, pL2, pR2, QL.b, QR.b, drytol, netL, netR, ms);
+    // p = net(2:3) T
+    fL.h = netL[0];
+    fL.p1 = z0(netL[1] * n1) + netL[2] * -n2;
+    fL.p2 = z0(netL[1] * n2) + netL[2] * n1;
+    fL.s = ms;
+    fR.h = netR[0];
+    fR.p1 = z0(netR[1] * n1) + netR[2] * -n2;
+    fR.p2 = z0(netR[1] * n2) + netR[2] * n1;
+    fR.s = ms;
+}
+
+__device__ __forceinline__ double normal_velocity(double n1, double n2, double p1, double p2, double d) {
+    return z0(n1 * (p1 / d)) + n2 * (p2 / d);
+}
+
+// compute_lf_flux, src/SWE/SWE_euler_timestep.f90:359-446
+template <int SOLVER>
+__device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, const State& QR, double drytol,
+                                        Update& fL, Update& fR) {
+    const double g = kG;
+    if (SOLVER == LF_BATH || SOLVER == LLF_BATH) {
+        double dL = QL.h - QL.b, dR = QR.h - QR.b;
+        if (dL < drytol || dR < drytol) {
+            fL = Update{0.0, 0.0, 0.0, 0.0};
+            fR = Update{0.0, 0.0, 0.0, 0.0};
+            if (dL < drytol && dR < drytol) {
+            } else if (dL < drytol) {
+                double hR = dmx(dR, 0.0);
+                double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+                fR.s = sqrt(g * hR) + fabs(vR);
+                double pr = ((0.5 * g) * hR) * hR;
+                fR.p1 = (-((0.5 * vR) * QR.p1) - pr * n1) + (0.5 * fR.s) * QR.p1;
+                fR.p2 = (-((0.5 * vR) * QR.p2) - pr * n2) + (0.5 * fR.s) * QR.p2;
+            } else {
+                double hL = dmx(dL, 0.0);
+                double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
+                fL.s = sqrt(g * hL) + fabs(vL);
+                double pr = ((0.5 * g) * hL) * hL;
+                fL.p1 = ((0.5 * vL) * QL.p1 + pr * n1) + (0.5 * fL.s) * QL.p1;
+                fL.p2 = ((0.5 * vL) * QL.p2 + pr * n2) + (0.5 * fL.s) * QL.p2;
+            }
+            return;
+        }
+        double hL = dmx(dL, 0.0), hR = dmx(dR, 0.0);
+        double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
+        double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+        fL.s = sqrt(g * hL) + fabs(vL);
+        fR.s = sqrt(g * hR) + fabs(vR);
+        double alpha = (SOLVER == LLF_BATH) ? dmx(fL.s, fR.s) : 100.0;
+        fL.h = 0.5 * ((hL * vL + hR * vR) + alpha * (QL.h - QR.h));
+        fR.h = -fL.h;
+        double pr = (0.5 * g) * (hL * hL + hR * hR);
+        fL.p1 = 0.5 * (((QL.p1 * vL + QR.p1 * vR) + pr * n1) + alpha * (QL.p1 - QR.p1));
+        fL.p2 = 0.5 * (((QL.p2 * vL + QR.p2 * vR) + pr * n2) + alpha * (QL.p2 - QR.p2));
+        fR.p1 = -fL.p1;
+        fR.p2 = -fL.p2;
+        double src = ((0.25 * g) * (hL + hR)) * (QR.b - QL.b);
+        fL.p1 = fL.p1 + src * n1;
+        fL.p2 = fL.p2 + src * n2;
+        fR.p1 = fR.p1 + src * n1;
+        fR.p2 = fR.p2 + src * n2;
+    } else {
+        double dL = QL.h - 0.0, dR = QR.h - 0.0;
+        double hL = dmx(dL, 0.0), hR = dmx(dR, 0.0);
+        double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
+        double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+        fL.s = sqrt(g * dL) + fabs(vL);
+        fR.s = sqrt(g * dR) + fabs(vR);
+        double alpha = (SOLVER == LLF) ? dmx(fL.s, fR.s) : 100.0;
+        fL.h = 0.5 * ((vL * hL + vR * hR) + alpha * (QL.h - QR.h));
+        fR.h = -fL.h;
+        double sc = (vL * vL) * hL + (vR * vR) * hR;
+        double pr = (0.5 * g) * (hL * hL + hR * hR);
+        fL.p1 = 0.5 * ((sc + pr * n1) + alpha * (QL.p1 - QR.p1));
+        fL.p2 = 0.5 * ((sc + pr * n2) + alpha * (QL.p2 - QR.p2));
+        fR.p1 = -fL.p1;
+        fR.p2 = -fL.p2;
+    }
+}
+
+template <int SOLVER>
+__device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL, const State& QR, double drytol,
+                                          Update& fL, Update& fR) {
+    if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
+        geoclaw_flux<SOLVER>(n1, n2, QL, QR, drytol, fL, fR);
+    else
+        lf_flux<SOLVER>(n1, n2, QL, QR, drytol, fL, fR);
+}
+
+// Ghost state of bnd_skeleton_scalar_op, src/SWE/SWE_euler_timestep.f90:231-255.
+template <int BC>
+__device__ __forceinline__ State boundary_ghost(double n1, double n2, const State& Q) {
+    State g = Q;
+    if (BC == BC_SLIP) {
+        double d = z0(Q.p1 * n1) + Q.p2 * n2;
+        g.p1 = Q.p1 - d * n1;
+        g.p2 = Q.p2 - d * n2;
+    } else if (BC == BC_NOSLIP) {
+        g.p1 = -Q.p1;
+        g.p2 = -Q.p2;
+    }
+    return g;
+}
+
+}  // namespace swe

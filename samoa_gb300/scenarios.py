@@ -1,0 +1,136 @@
+"""Synthetic SWE scenarios on uniform Sierpinski meshes (host-side setup).
+
+The reference hard-codes a 1-D dam break on flat bathymetry or reads NetCDF
+bathymetry through ASAGI (src/SWE/SWE_initialize.f90:120-185,349-370); the
+workloads here are seeded synthetic generators of the same kind. Reference
+depth d has 2^(d+1) cells (src/SFC_node_traversal.f90:46), so "2^k cells" is
+reference depth k - 1. States are sampled at cell centroids; h is the surface
+elevation (depth = h - b).
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+from .swe import Config, Grid, initial_dt, uniform_mesh
+
+
+@dataclass
+class Scenario:
+    name: str
+    grid: Grid
+    cfg: Config
+    steps: int
+
+
+def _world(mesh, cfg):
+    c = mesh.centroids
+    return cfg.scaling * c[:, 0] + cfg.offset[0], cfg.scaling * c[:, 1] + cfg.offset[1]
+
+
+def _grid(mesh, cfg, h, b):
+    n = mesh.n_cells
+    hu = np.zeros(n)
+    hv = np.zeros(n)
+    g = Grid(mesh, np.ascontiguousarray(h, np.float64), hu, hv, np.ascontiguousarray(b, np.float64))
+    g.r_dt = initial_dt(mesh, g.h, hu, hv, g.b, cfg.courant_number)
+    return g
+
+
+def radial_dam_break(log2_cells=16, boundary="slip", solver="fwave", mesh=None):
+    """Radial dam break on [-0.5, 0.5]^2: flat b = -10 m, water depth 15 m inside
+    r < 0.1 and 10 m elsewhere, at rest; CFL 0.5, 100 steps, no adaptivity."""
+    d = log2_cells - 1
+    cfg = Config(flux_solver=solver, boundary=boundary, courant_number=0.5, dry_tolerance=0.01, scaling=1.0,
+                 offset=(-0.5, -0.5), i_min_depth=d, i_max_depth=d)
+    mesh = mesh or uniform_mesh(d)
+    x, y = _world(mesh, cfg)
+    b = np.full(mesh.n_cells, -10.0)
+    h = b + np.where(np.hypot(x, y) < 0.1, 15.0, 10.0)
+    return Scenario("radial_dam_break", _grid(mesh, cfg, h, b), cfg, 100)
+
+
+def bowl_bathymetry(x, y, h0=10.0, a=0.4):
+    r2 = x * x + y * y
+    return -h0 * (1.0 - r2 / (a * a))
+
+
+def parabolic_bowl(log2_cells=14, seed=2, solver="aug_riemann", amplitude=0.5, sigma=0.05, mesh=None,
+                   min_depth=None, max_depth=None):
+    """Parabolic bowl b(r) = -10 (1 - r^2 / 0.4^2) on [-0.5, 0.5]^2 (dry land for
+    r > 0.4) with a Gaussian surface bump at a seeded offset; dry tolerance 1e-3 m.
+    On a frozen uniform mesh (the remeshing of the adaptive case stays on the host)."""
+    d = log2_cells - 1
+    cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=1e-3, scaling=1.0,
+                 offset=(-0.5, -0.5), i_min_depth=d if min_depth is None else min_depth,
+                 i_max_depth=d + 1 if max_depth is None else max_depth)
+    mesh = mesh or uniform_mesh(d)
+    x, y = _world(mesh, cfg)
+    rng = np.random.default_rng(seed)
+    x0, y0 = rng.uniform(-0.1, 0.1, 2)
+    b = bowl_bathymetry(x, y)
+    eta = amplitude * np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / (2 * sigma * sigma))
+    # surface = eta over water; on land the state is dry: h = b (depth 0)
+    h = np.where(b < eta, eta, b)
+    return Scenario("parabolic_bowl", _grid(mesh, cfg, h, b), cfg, 500)
+
+
+def _hash2(ix, iy, seed):
+    v = (ix.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)) ^ (iy.astype(np.uint64) * np.uint64(0xC2B2AE3D27D4EB4F))
+    v ^= np.uint64(seed) * np.uint64(0x165667B19E3779F9)
+    v ^= v >> np.uint64(31)
+    v *= np.uint64(0xBF58476D1CE4E5B9)
+    v ^= v >> np.uint64(29)
+    return (v >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0) * 2.0 - 1.0
+
+
+def value_noise(x, y, seed, octaves=5, base=8.0, persistence=0.5):
+    """Seeded lattice value noise in [-1, 1] with smooth-step interpolation, summed over octaves."""
+    out = np.zeros_like(x)
+    amp, freq, norm = 1.0, base, 0.0
+    with np.errstate(over="ignore"):
+        for o in range(octaves):
+            fx, fy = x * freq, y * freq
+            ix, iy = np.floor(fx), np.floor(fy)
+            tx, ty = fx - ix, fy - iy
+            ix = ix.astype(np.int64) + (1 << 20)
+            iy = iy.astype(np.int64) + (1 << 20)
+            sx, sy = tx * tx * (3 - 2 * tx), ty * ty * (3 - 2 * ty)
+            s = seed * 1000 + o
+            v00, v10 = _hash2(ix, iy, s), _hash2(ix + 1, iy, s)
+            v01, v11 = _hash2(ix, iy + 1, s), _hash2(ix + 1, iy + 1, s)
+            out += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sy) + (v01 * (1 - sx) + v11 * sx) * sy)
+            norm += amp
+            amp *= persistence
+            freq *= 2.0
+    return out / norm
+
+
+def ocean_basin(log2_cells=26, seed=3, solver="fwave", steps=200, mesh=None, scaling=1.0e6):
+    """Synthetic ocean basin: tanh shelf from a -4000 m abyssal plain to a -50 m
+    shelf plus 200 m of 5-octave seeded value noise, a Gaussian uplift of 2 m
+    with sigma 2 % of the domain width at a seeded centre; f-wave, outflow."""
+    d = log2_cells - 1
+    cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=0.01, scaling=scaling,
+                 offset=(-0.5 * scaling, -0.5 * scaling), i_min_depth=d, i_max_depth=d)
+    mesh = mesh or uniform_mesh(d)
+    u = mesh.centroids[:, 0] - 0.5
+    v = mesh.centroids[:, 1] - 0.5
+    rng = np.random.default_rng(seed)
+    x0, y0 = rng.uniform(-0.25, 0.1, 2)
+    b = -4000.0 + 3950.0 * 0.5 * (1.0 + np.tanh((u - 0.25) / 0.05)) + 200.0 * value_noise(u, v, seed)
+    b = np.minimum(b, -20.0)  # keep the shelf under water
+    eta = 2.0 * np.exp(-((u - x0) ** 2 + (v - y0) ** 2) / (2 * 0.02 * 0.02))
+    h = b + (eta - b)  # surface elevation eta over the bathymetry
+    return Scenario("ocean_basin", _grid(mesh, cfg, h, b), cfg, steps)
+
+
+def lake_at_rest(log2_cells=10, solver="fwave", seed=7, mesh=None):
+    """Flat surface at 0 over rough bathymetry, at rest: the well-balanced solvers keep it exactly."""
+    d = log2_cells - 1
+    cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=0.01, scaling=1.0,
+                 offset=(-0.5, -0.5), i_min_depth=0, i_max_depth=d + 1)
+    mesh = mesh or uniform_mesh(d)
+    x, y = _world(mesh, cfg)
+    b = -5.0 + 2.0 * value_noise(x + 0.5, y + 0.5, seed, octaves=3)
+    h = np.zeros(mesh.n_cells)
+    return Scenario("lake_at_rest", _grid(mesh, cfg, h, b), cfg, 10)

@@ -1,0 +1,269 @@
+"""Host-side mirror of sam(oa)^2's SWE Euler time-step traversal over the C ABI.
+
+The reference calls ``swe%euler%traverse(grid)`` once per time step
+(src/SWE/SWE.f90:393). Here a :class:`Grid` holds the Sierpinski mesh and the
+cell state ``Q = (h, hu, hv, b)`` (h is the surface elevation, depth = h - b,
+src/SWE/SWE_data_types.f90:42-65) plus ``r_time``, ``r_dt`` and ``r_dt_new``;
+:class:`SweEulerTimestepTraversal` runs the step on the GPU through
+libsamoa_swe.so and leaves the grid updated, with refinement flags and
+``i_refinements_issued`` like the reference traversal.
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+FWAVE, AUG_RIEMANN, LF, LF_BATH, LLF, LLF_BATH = 1, 3, 10, 11, 12, 13
+SOLVERS = {"fwave": FWAVE, "aug_riemann": AUG_RIEMANN, "lf": LF, "lfbath": LF_BATH, "llf": LLF,
+           "llfbath": LLF_BATH}
+BC_OUTFLOW, BC_SLIP, BC_NOSLIP = 0, 1, 2
+BOUNDARIES = {"outflow": BC_OUTFLOW, "slip": BC_SLIP, "noslip": BC_NOSLIP}
+
+G = 9.80665  # src/SWE/SWE_data_types.f90:34
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+@dataclass
+class Config:
+    """The cfg fields the step reads (src/Config.f90:30-121; SWE defaults of :183)."""
+    flux_solver: str = "fwave"
+    boundary: str = "outflow"
+    courant_number: float = 0.45
+    dry_tolerance: float = 0.01
+    scaling: float = 1.0
+    offset: tuple = (0.0, 0.0)
+    i_min_depth: int = 0
+    i_max_depth: int = 14
+    r_max_time: float = -1.0
+    r_output_time_step: float = -1.0
+
+    def params(self):
+        return _lib.SweParams(SOLVERS[self.flux_solver], BOUNDARIES[self.boundary], self.dry_tolerance,
+                              self.courant_number, self.scaling, self.i_min_depth, self.i_max_depth,
+                              self.r_max_time, self.r_output_time_step)
+
+
+@dataclass
+class Mesh:
+    """Cells in traversal order and their edge streams (the C-ABI layout)."""
+    depth: np.ndarray          # int8[n]
+    plotter: np.ndarray        # int8[n]
+    edge_cells: np.ndarray     # int64[ne, 2]
+    edge_local: np.ndarray     # int8[ne, 2], 1..3
+    bnd_cell: np.ndarray       # int64[nb]
+    bnd_local: np.ndarray      # int8[nb]
+    centroids: np.ndarray = None  # float64[n, 2] in the unit square (optional)
+    version: int = 0
+
+    @property
+    def n_cells(self):
+        return len(self.depth)
+
+
+def uniform_mesh(depth, centroids=True):
+    """Uniform Sierpinski mesh of the unit square at reference depth ``depth`` (2^(depth+1) cells)."""
+    L = _lib.load()
+    n, ne, nb = C.c_int64(), C.c_int64(), C.c_int64()
+    _lib.check(L.swe_mesh_uniform(depth, C.byref(n), C.byref(ne), C.byref(nb), *([None] * 8)))
+    n, ne, nb = n.value, ne.value, nb.value
+    d = np.empty(n, np.int8)
+    p = np.empty(n, np.int8)
+    ec = np.empty((ne, 2), np.int64)
+    el = np.empty((ne, 2), np.int8)
+    bc = np.empty(nb, np.int64)
+    bl = np.empty(nb, np.int8)
+    cen = np.empty((n, 2), np.float64) if centroids else None
+    _lib.check(L.swe_mesh_uniform(depth, None, None, None, _p(d), _p(p), _p(ec), _p(el), _p(bc), _p(bl), _p(cen)))
+    return Mesh(d, p, ec, el, bc, bl, cen)
+
+
+@dataclass
+class Grid:
+    """A mesh plus the SWE cell state and the time-stepping scalars of t_grid."""
+    mesh: Mesh
+    h: np.ndarray
+    hu: np.ndarray
+    hv: np.ndarray
+    b: np.ndarray
+    r_time: float = 0.0
+    r_dt: float = 0.0
+    r_dt_new: float = 0.0
+    refinement: np.ndarray = None
+    i_refinements_issued: int = 0
+    steps_since_upload: int = 0
+    _dirty: bool = field(default=True, repr=False)
+
+    def mark_dirty(self):
+        """Call after changing the host state arrays so the next traverse uploads them."""
+        self._dirty = True
+
+
+class SweContext:
+    """Owner of one swe_ctx (device buffers, stream, device scalars)."""
+
+    def __init__(self, device=0):
+        self.L = _lib.load()
+        self.ptr = C.c_void_p()
+        _lib.check(self.L.swe_create(C.byref(self.ptr), device))
+        self.n_cells = 0
+
+    def close(self):
+        if self.ptr:
+            self.L.swe_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        _lib.check(self.L.swe_set_params(self.ptr, C.byref(params)))
+
+    def set_stream(self, stream_handle):
+        _lib.check(self.L.swe_set_stream(self.ptr, C.c_void_p(stream_handle)))
+
+    def set_tiling(self, segment_cells=0, block_threads=0):
+        _lib.check(self.L.swe_set_tiling(self.ptr, segment_cells, block_threads))
+
+    def get_tiling(self):
+        a, b = C.c_int32(), C.c_int32()
+        _lib.check(self.L.swe_get_tiling(self.ptr, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def upload_mesh(self, mesh):
+        ec = np.ascontiguousarray(mesh.edge_cells, np.int64)
+        el = np.ascontiguousarray(mesh.edge_local, np.int8)
+        bc = np.ascontiguousarray(mesh.bnd_cell, np.int64)
+        bl = np.ascontiguousarray(mesh.bnd_local, np.int8)
+        d = np.ascontiguousarray(mesh.depth, np.int8)
+        p = np.ascontiguousarray(mesh.plotter, np.int8)
+        _lib.check(self.L.swe_mesh_upload(self.ptr, len(d), _p(d), _p(p), len(ec), _p(ec), _p(el), len(bc), _p(bc),
+                                          _p(bl)))
+        self.n_cells = len(d)
+
+    def upload_state(self, h, hu, hv, b):
+        arrs = [np.ascontiguousarray(x, np.float64) for x in (h, hu, hv, b)]
+        for a in arrs:
+            if a.shape != (self.n_cells,):
+                raise ValueError("state arrays must have shape (%d,)" % self.n_cells)
+        _lib.check(self.L.swe_state_upload(self.ptr, *[_p(a) for a in arrs]))
+
+    def download_state(self, out=None):
+        if out is None:
+            out = [np.empty(self.n_cells, np.float64) for _ in range(4)]
+        _lib.check(self.L.swe_state_download(self.ptr, *[_p(a) for a in out]))
+        return out
+
+    def device_state(self):
+        ptrs = [C.c_void_p() for _ in range(4)]
+        _lib.check(self.L.swe_state_device(self.ptr, *[C.byref(q) for q in ptrs]))
+        return [q.value for q in ptrs]
+
+    def set_time(self, time, dt):
+        _lib.check(self.L.swe_set_time(self.ptr, float(time), float(dt)))
+
+    def get_time(self):
+        t, dt, dn = C.c_double(), C.c_double(), C.c_double()
+        _lib.check(self.L.swe_get_time(self.ptr, C.byref(t), C.byref(dt), C.byref(dn)))
+        return t.value, dt.value, dn.value
+
+    def traverse(self, n_steps=1):
+        _lib.check(self.L.swe_traverse(self.ptr, int(n_steps)))
+
+    def refinements(self, flags=None):
+        if flags is None:
+            flags = np.empty(self.n_cells, np.int8)
+        n = C.c_int64()
+        _lib.check(self.L.swe_get_refinements(self.ptr, _p(flags), C.byref(n)))
+        return flags, n.value
+
+    def step_count(self):
+        s = C.c_int64()
+        _lib.check(self.L.swe_get_step_count(self.ptr, C.byref(s)))
+        return s.value
+
+    def synchronize(self):
+        _lib.check(self.L.swe_synchronize(self.ptr))
+
+
+class SweEulerTimestepTraversal:
+    """GPU drop-in for t_swe_euler_timestep_traversal (src/SWE/SWE_euler_timestep.f90).
+
+    ``traverse(grid)`` performs one explicit Euler step exactly like
+    ``swe%euler%traverse(grid)``: uses ``grid.r_dt``, advances ``grid.r_time``,
+    sets ``grid.r_dt = courant * min(volume / sum(len * speed))``, the
+    refinement flags and ``grid.i_refinements_issued``. The mesh is uploaded
+    when its ``version`` changes (a remesh), the state when the grid is dirty.
+    With ``sync_state=False`` the state stays on the device between calls
+    (call :meth:`fetch` to read it back).
+    """
+
+    def __init__(self, cfg: Config, device=0):
+        self.cfg = cfg
+        self.ctx = SweContext(device)
+        self.ctx.set_params(cfg.params())
+        self._mesh_key = None
+
+    def set_tiling(self, segment_cells=0, block_threads=0):
+        self.ctx.set_tiling(segment_cells, block_threads)
+
+    def _ensure(self, grid):
+        key = (id(grid.mesh), grid.mesh.version)
+        if key != self._mesh_key:
+            self.ctx.upload_mesh(grid.mesh)
+            self._mesh_key = key
+            grid._dirty = True
+            grid.steps_since_upload = 0
+        if grid._dirty:
+            self.ctx.upload_state(grid.h, grid.hu, grid.hv, grid.b)
+            self.ctx.set_time(grid.r_time, grid.r_dt)
+            grid._dirty = False
+
+    def traverse(self, grid: Grid, steps=1, sync_state=True, flags=True):
+        self.ctx.set_params(self.cfg.params())
+        self._ensure(grid)
+        self.ctx.traverse(steps)
+        grid.steps_since_upload += steps
+        self.ctx.synchronize()
+        grid.r_time, grid.r_dt, grid.r_dt_new = self.ctx.get_time()
+        if flags:
+            grid.refinement, grid.i_refinements_issued = self.ctx.refinements(grid.refinement)
+        if sync_state:
+            self.fetch(grid)
+        return grid
+
+    def fetch(self, grid: Grid):
+        out = [grid.h, grid.hu, grid.hv, grid.b]
+        out = [o if (o is not None and o.flags.c_contiguous and o.dtype == np.float64) else
+               np.empty(self.ctx.n_cells) for o in out]
+        self.ctx.download_state(out)
+        grid.h, grid.hu, grid.hv, grid.b = out
+        return grid
+
+    def close(self):
+        self.ctx.close()
+
+
+def initial_dt(mesh: Mesh, h, hu, hv, b, courant):
+    """Initial time step of the init_dofs traversal (src/SWE/SWE_initialize.f90:325-335):
+    courant * min(volume / (sum(edge sizes) * max wave speed)), with the unscaled
+    cell geometry the reference uses there."""
+    from .geometry import leg_sizes, volumes
+    d = mesh.depth.astype(np.int64)
+    leg = leg_sizes()
+    vol = volumes()[d]
+    edges = (leg[d + 1] + leg[d]) + leg[d + 1]
+    depth = h - b
+    wet = depth > 0.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        speed = np.where(wet, np.sqrt(G * depth) + np.sqrt((hu * hu + hv * hv) / (depth * depth)), 0.0)
+        dt = vol / (edges * speed)
+    dt = np.where(np.isnan(dt), np.inf, dt)
+    return courant * min(float(np.min(dt)), np.finfo(np.float64).max)

@@ -1,0 +1,45 @@
+"""Shared helpers of the parity tests: run a scenario on the GPU (through the C
+ABI) and on the oracle, and compare bit for bit."""
+import numpy as np
+
+from oracle import oracle as O
+from samoa_gb300 import swe
+
+
+def oracle_params(cfg):
+    return O.make_params(solver=swe.SOLVERS[cfg.flux_solver], bc=swe.BOUNDARIES[cfg.boundary],
+                         dry_tolerance=cfg.dry_tolerance, courant=cfg.courant_number, scaling=cfg.scaling,
+                         min_depth=cfg.i_min_depth, max_depth=cfg.i_max_depth, max_time=cfg.r_max_time,
+                         output_time_step=cfg.r_output_time_step)
+
+
+def walk_state(mesh_depth, grid):
+    """Oracle walk over the reference's cell grammar for a uniform mesh."""
+    om = O.mesh_uniform(mesh_depth)
+    return O.WalkState(om["cells5"], grid.h, grid.hu, grid.hv, grid.b, grid.r_time, grid.r_dt)
+
+
+def omp_state(mesh, grid, parity=0):
+    return O.OmpState(mesh.depth, mesh.plotter, mesh.edge_cells, mesh.edge_local, mesh.bnd_cell, mesh.bnd_local,
+                      grid.h, grid.hu, grid.hv, grid.b, grid.r_time, grid.r_dt, parity)
+
+
+def same_bits(a, b):
+    """Equal as values (so +0.0 == -0.0), NaN nowhere."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return a.shape == b.shape and not np.isnan(a).any() and not np.isnan(b).any() and bool(np.all(a == b))
+
+
+def assert_state_equal(tag, h, hu, hv, ref_h, ref_hu, ref_hv):
+    for name, x, y in (("h", h, ref_h), ("hu", hu, ref_hu), ("hv", hv, ref_hv)):
+        if not same_bits(x, y):
+            d = np.abs(np.asarray(x) - np.asarray(y))
+            i = int(np.nanargmax(d))
+            raise AssertionError("%s: %s differs at %d cells, max |diff| %.3e at cell %d (%r vs %r)" %
+                                 (tag, name, int((d != 0).sum()), float(d[i]), i, float(x[i]), float(y[i])))
+
+
+def rel_l2(a, b):
+    den = max(float(np.linalg.norm(b)), 1e-300)
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b))) / den

@@ -1,0 +1,211 @@
+"""GPU parity of the fused SWE step against the oracle, through the C ABI.
+
+Bar: bit-exact state (h, hu, hv), refinement flags, refinement count, time and
+dt after every step, for every solver and boundary condition, against the
+sequential walk that follows the reference traversal (cell grammar reversed
+every step). At sizes the walk cannot reach in seconds the OpenMP oracle
+(checked against the walk bit for bit in test_oracle.py) is the reference.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from samoa_gb300 import scenarios, swe
+
+from .helpers import assert_state_equal, omp_state, oracle_params, walk_state
+
+pytestmark = pytest.mark.gpu
+
+
+def run_compare_walk(scn, steps, tiling=None):
+    g = scn.grid
+    depth = int(g.mesh.depth[0])
+    W = walk_state(depth, g)
+    P = oracle_params(scn.cfg)
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    if tiling:
+        trav.set_tiling(*tiling)
+    try:
+        for k in range(steps):
+            W.steps(P, 1)
+            trav.traverse(g)
+            tag = "%s step %d" % (scn.name, k)
+            assert_state_equal(tag, g.h, g.hu, g.hv, W.h, W.hu, W.hv)
+            assert np.array_equal(g.refinement, W.flags), tag + ": refinement flags differ"
+            assert g.i_refinements_issued == W.n_refine, tag
+            assert g.r_time == W.time and g.r_dt == W.dt, (tag, g.r_time, W.time, g.r_dt, W.dt)
+            assert g.r_dt_new == W.dt_new, tag
+    finally:
+        trav.close()
+
+
+@pytest.mark.parametrize("boundary", ["slip", "outflow", "noslip"])
+def test_dam_break_fwave_bitexact(swe_lib, oracle_lib, boundary):
+    scn = scenarios.radial_dam_break(log2_cells=12, boundary=boundary)
+    run_compare_walk(scn, 12)
+
+
+@pytest.mark.parametrize("solver", ["aug_riemann", "fwave", "llfbath", "lfbath"])
+def test_bowl_wet_dry_bitexact(swe_lib, oracle_lib, solver):
+    scn = scenarios.parabolic_bowl(log2_cells=12, solver=solver, amplitude=2.0, sigma=0.08)
+    run_compare_walk(scn, 15)
+
+
+@pytest.mark.parametrize("solver", ["lf", "llf"])
+def test_lf_flat_bitexact(swe_lib, oracle_lib, solver):
+    # the LF fluxes without bathymetry assume b = 0 (src/SWE/SWE_euler_timestep.f90:423)
+    scn = scenarios.radial_dam_break(log2_cells=10, boundary="outflow", solver=solver)
+    g = scn.grid
+    g.b[:] = 0.0
+    g.h[:] = g.h + 10.0
+    g.r_dt = swe.initial_dt(g.mesh, g.h, g.hu, g.hv, g.b, scn.cfg.courant_number)
+    run_compare_walk(scn, 10)
+
+
+def test_refinement_flags_bitexact(swe_lib, oracle_lib):
+    # dmin < depth < dmax so both refine and coarsen flags occur
+    scn = scenarios.radial_dam_break(log2_cells=12, boundary="slip")
+    scn.cfg.i_min_depth = 5
+    scn.cfg.i_max_depth = 13
+    run_compare_walk(scn, 8)
+
+
+@pytest.mark.parametrize("tiling", [(64, 64), (96, 128), (2048, 256), (1024, 256), (256, 96)])
+def test_tilings_bitexact(swe_lib, oracle_lib, tiling):
+    scn = scenarios.parabolic_bowl(log2_cells=13, amplitude=1.0)
+    run_compare_walk(scn, 6, tiling=tiling)
+
+
+def test_dt_clamps(swe_lib, oracle_lib):
+    scn = scenarios.radial_dam_break(log2_cells=10)
+    scn.cfg.r_max_time = 1e-4
+    scn.cfg.r_output_time_step = 5e-5
+    run_compare_walk(scn, 5)
+
+
+def test_large_mesh_against_omp(swe_lib, oracle_lib):
+    scn = scenarios.ocean_basin(log2_cells=20, steps=6)
+    g = scn.grid
+    S = omp_state(g.mesh, g)
+    P = oracle_params(scn.cfg)
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    try:
+        for k in range(4):
+            S.steps(P, 1)
+            trav.traverse(g)
+            assert_state_equal("basin step %d" % k, g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+            assert g.r_dt == S.scal[1] and g.r_time == S.scal[0]
+    finally:
+        trav.close()
+
+
+def _odd_mesh(depth):
+    """A uniform mesh with its last cell removed: odd cell count, the removed
+    cell's neighbours get boundary edges instead. Exercises ragged segments."""
+    m = swe.uniform_mesh(depth)
+    n = m.n_cells - 1
+    keep = (m.edge_cells[:, 0] < n) & (m.edge_cells[:, 1] < n)
+    ec, el = m.edge_cells[keep], m.edge_local[keep]
+    cut = ~keep
+    nb_c = np.where(m.edge_cells[cut, 0] < n, m.edge_cells[cut, 0], m.edge_cells[cut, 1])
+    nb_l = np.where(m.edge_cells[cut, 0] < n, m.edge_local[cut, 0], m.edge_local[cut, 1])
+    bk = m.bnd_cell < n
+    bc = np.concatenate([m.bnd_cell[bk], nb_c])
+    bl = np.concatenate([m.bnd_local[bk], nb_l]).astype(np.int8)
+    return swe.Mesh(m.depth[:n].copy(), m.plotter[:n].copy(), ec.copy(), el.copy(), bc, bl, m.centroids[:n].copy())
+
+
+@pytest.mark.parametrize("tiling", [(64, 64), (512, 256)])
+def test_odd_cell_count_against_omp(swe_lib, oracle_lib, tiling):
+    mesh = _odd_mesh(9)
+    assert mesh.n_cells % 2 == 1
+    scn = scenarios.radial_dam_break(log2_cells=10, mesh=None)
+    n = mesh.n_cells
+    g = swe.Grid(mesh, scn.grid.h[:n].copy(), scn.grid.hu[:n].copy(), scn.grid.hv[:n].copy(), scn.grid.b[:n].copy(),
+                 0.0, scn.grid.r_dt)
+    S = omp_state(mesh, g)
+    P = oracle_params(scn.cfg)
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    trav.set_tiling(*tiling)
+    try:
+        for k in range(6):
+            S.steps(P, 1)
+            trav.traverse(g)
+            assert_state_equal("odd mesh step %d" % k, g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+            assert np.array_equal(g.refinement, S.flags)
+    finally:
+        trav.close()
+
+
+def test_lake_at_rest_is_exact(swe_lib):
+    scn = scenarios.lake_at_rest(log2_cells=12)
+    g = scn.grid
+    h0 = g.h.copy()
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    try:
+        trav.traverse(g, steps=20)
+        assert np.array_equal(g.h, h0)
+        assert not g.hu.any() and not g.hv.any()
+    finally:
+        trav.close()
+
+
+def test_mass_conservation_and_drift(swe_lib, oracle_lib):
+    """Mass is conserved to round-off (reflective walls, no wet/dry clamps);
+    after 1,000 steps the GPU state still equals the oracle's bit for bit."""
+    scn = scenarios.radial_dam_break(log2_cells=12, boundary="noslip")
+    g = scn.grid
+    vol = O.cell_volume(int(g.mesh.depth[0]))
+    m0 = float(np.sum(g.h - g.b)) * vol
+    S = omp_state(g.mesh, g)
+    P = oracle_params(scn.cfg)
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    try:
+        trav.traverse(g, steps=1000)
+        S.steps(P, 1000)
+        assert_state_equal("after 1000 steps", g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+        m1 = float(np.sum(g.h - g.b)) * vol
+        # noslip ghost mirrors the momentum, so the boundary mass flux is round-off only
+        assert abs(m1 - m0) / m0 < 1e-11, (m0, m1)
+    finally:
+        trav.close()
+
+
+def test_determinism(swe_lib):
+    out = []
+    for _ in range(2):
+        scn = scenarios.parabolic_bowl(log2_cells=14, amplitude=1.0)
+        trav = swe.SweEulerTimestepTraversal(scn.cfg)
+        trav.traverse(scn.grid, steps=25)
+        trav.close()
+        out.append(np.concatenate([scn.grid.h, scn.grid.hu, scn.grid.hv]).view(np.uint64))
+    assert np.array_equal(out[0], out[1])
+
+
+def test_riemann_batch_against_oracle(swe_lib, oracle_lib):
+    """Solver-level check on targeted edge states: wet/wet, dry/dry, wet/dry,
+    walls, supercritical flow, transcritical, random normals."""
+    import ctypes as C
+    from samoa_gb300 import _lib
+    rng = np.random.default_rng(11)
+    n = 4000
+    normals = rng.normal(size=(n, 2))
+    normals /= np.linalg.norm(normals, axis=1, keepdims=True)
+    bl = rng.uniform(-20, 5, n)
+    br = bl + rng.choice([0.0, 1.0], n) * rng.uniform(-10, 10, n)
+    dl = rng.choice([0.0, 1e-4, 1.0], n, p=[0.2, 0.1, 0.7]) * rng.uniform(0, 20, n)
+    dr = rng.choice([0.0, 1e-4, 1.0], n, p=[0.2, 0.1, 0.7]) * rng.uniform(0, 20, n)
+    ql = np.stack([bl + dl, rng.normal(0, 30, n), rng.normal(0, 30, n), bl], 1)
+    qr = np.stack([br + dr, rng.normal(0, 30, n), rng.normal(0, 30, n), br], 1)
+    drytol = 1e-3
+    L = _lib.load()
+    for solver in (swe.FWAVE, swe.AUG_RIEMANN, swe.LF_BATH, swe.LLF_BATH):
+        gl, gr = np.zeros((n, 4)), np.zeros((n, 4))
+        p = lambda a: np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
+        _lib.check(L.swe_riemann_batch(solver, n, p(normals), p(ql), p(qr), drytol, p(gl), p(gr)))
+        ol, orr = np.zeros((n, 4)), np.zeros((n, 4))
+        for i in range(n):
+            ol[i], orr[i] = O.edge_flux(solver, normals[i], ql[i], qr[i], drytol)
+        ok = np.isfinite(ol).all(1) & np.isfinite(orr).all(1)
+        assert np.array_equal(gl[ok], ol[ok]) and np.array_equal(gr[ok], orr[ok]), solver
+        assert np.array_equal(np.isfinite(gl).all(1) & np.isfinite(gr).all(1), ok), solver
