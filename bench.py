@@ -1,0 +1,347 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 SWE time step: cell-updates/s and the HBM roofline.
+
+Workload: synthetic ocean basin, 2^26 = 67,108,864 cells (reference depth 25),
+uniform Sierpinski mesh, FP64, f-wave solver, outflow boundaries. One bench
+step is one explicit Euler time step over the whole mesh (the reference's
+``swe%euler%traverse(grid)``). The state (2.1 GB) is larger than L2, so no
+flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+N > 1 runs N independent replicas (one per GPU, launched by torchrun); the
+path does not shard across GPUs here ("replicas only"). ``--impl reference``
+times the CPU implementation of the step (the project's OpenMP restatement of
+the reference's FP64 step; the reference itself is Fortran and is not built)
+on the host cores, on a bounded sample of the workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL = 56  # read h, hu, hv, b + write h, hu, hv (FP64)
+METRIC = "swe_cell_updates_per_s"
+UNIT = "cell-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--log2-cells", type=int, default=26)
+    ap.add_argument("--solver", default="fwave")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-sample-log2", type=int, default=22)
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--segment-cells", type=int, default=0)
+    ap.add_argument("--block-threads", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def profile_figure(key):
+    """A figure from the committed ncu summary of the step kernel, or None."""
+    path = os.path.join(ROOT, "profiles", "swe_step_fwave_basin.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.strip().startswith(key + ":"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax = float(p[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(log2, steps, solver, threads):
+    """Time the OpenMP CPU step (the oracle's restatement of the reference step)
+    on a 2^log2-cell sample of the same basin workload."""
+    from oracle import oracle as O
+    from samoa_gb300 import scenarios, swe
+    scn = scenarios.ocean_basin(log2_cells=log2, solver=solver)
+    g = scn.grid
+    m = g.mesh
+    S = O.OmpState(m.depth, m.plotter, m.edge_cells, m.edge_local, m.bnd_cell, m.bnd_local, g.h, g.hu, g.hv, g.b,
+                   g.r_time, g.r_dt)
+    cfg = scn.cfg
+    P = O.make_params(solver=swe.SOLVERS[cfg.flux_solver], bc=swe.BOUNDARIES[cfg.boundary],
+                      dry_tolerance=cfg.dry_tolerance, courant=cfg.courant_number, scaling=cfg.scaling,
+                      min_depth=cfg.i_min_depth, max_depth=cfg.i_max_depth)
+    S.steps(P, 1, threads)  # warm-up
+    t0 = time.perf_counter()
+    S.steps(P, steps, threads)
+    t = time.perf_counter() - t0
+    return m.n_cells * steps / t, t
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    threads = O.max_threads()
+    per_step = []
+    total_cells = 0
+    # each bench step times a bounded sample (2^cpu_sample_log2 cells) of the workload
+    from samoa_gb300 import scenarios, swe
+    scn = scenarios.ocean_basin(log2_cells=a.cpu_sample_log2, solver=a.solver)
+    g = scn.grid
+    m = g.mesh
+    S = O.OmpState(m.depth, m.plotter, m.edge_cells, m.edge_local, m.bnd_cell, m.bnd_local, g.h, g.hu, g.hv, g.b,
+                   g.r_time, g.r_dt)
+    cfg = scn.cfg
+    P = O.make_params(solver=swe.SOLVERS[cfg.flux_solver], bc=swe.BOUNDARIES[cfg.boundary],
+                      dry_tolerance=cfg.dry_tolerance, courant=cfg.courant_number, scaling=cfg.scaling,
+                      min_depth=cfg.i_min_depth, max_depth=cfg.i_max_depth)
+    S.steps(P, a.warmup, threads)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        S.steps(P, 1, threads)
+        total_cells += m.n_cells
+    t = time.perf_counter() - t0
+    value = total_cells / t
+    sample = "2^%d-cell sample of the basin workload per step (%d cells), %d steps, OpenMP C restatement" % (
+        a.cpu_sample_log2, m.n_cells, a.steps)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1000.0 * t / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "solver": a.solver,
+                   "sample_cells": m.n_cells},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def fp64_dgemm_tflops(torch):
+    """Measured FP64 peak on this GPU: cuBLAS DGEMM 8192^3, best of 3."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def run_gpu(a, rank, world, local):
+    import torch
+    import torch.distributed as dist
+
+    from samoa_gb300 import build as lib_build
+    lib_build.build()
+    from samoa_gb300 import scenarios, swe
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    scn = scenarios.ocean_basin(log2_cells=a.log2_cells, solver=a.solver, device="cuda")
+    g = scn.grid
+    n = g.mesh.n_cells
+    ctx = swe.SweContext(local)
+    ctx.set_params(scn.cfg.params())
+    if a.segment_cells or a.block_threads:
+        ctx.set_tiling(a.segment_cells, a.block_threads)
+    ctx.upload_mesh(g.mesh)
+    ctx.upload_state(g.h, g.hu, g.hv, g.b)
+    ctx.set_time(g.r_time, g.r_dt)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    tiling = ctx.get_tiling()
+
+    # warm-up
+    ctx.traverse(a.warmup)
+    ctx.synchronize()
+
+    # timed region: K steps, CUDA events on the launching stream
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.traverse(a.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ctx.synchronize()  # raises if a kernel reported an error
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    sim_time, dt, _ = ctx.get_time()
+    value = n * a.steps * world / (ms * 1e-3)
+
+    # end to end through the public API with host buffers: every step uploads
+    # the state from pinned host memory, runs the step, reads the state and the
+    # refinement flags back
+    e2e = None
+    if not a.no_e2e:
+        pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()
+        hh, hu, hv, hb = (pin(x) for x in ctx.download_state())
+        flags = pin(np.zeros(n, np.int8))
+        ctx.traverse(1)
+        ctx.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(a.e2e_steps):
+            ctx.upload_state(hh, hu, hv, hb)
+            ctx.traverse(1)
+            ctx.download_state([hh, hu, hv, hb])
+            ctx.refinements(flags)
+        te = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([te], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": n * a.e2e_steps * world / te, "unit": UNIT, "h2d_bytes_per_step": 32 * n,
+               "d2h_bytes_per_step": 32 * n + n + 40, "steps": a.e2e_steps,
+               "note": "state upload from pinned host memory + step + state and flags download, every step"}
+
+    peaks, peak_kind = measured_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = BYTES_PER_CELL * n / (ms * 1e-3 / a.steps) / 1e9
+    traffic_per_cell = profile_figure("dram_bytes_per_cell")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_per_cell * n if traffic_per_cell else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (%s)" % peak_kind,
+                "algorithmic_bytes_per_cell": BYTES_PER_CELL}
+
+    out = None
+    if rank == 0:
+        fp64 = fp64_dgemm_tflops(torch)
+        fp64_util = profile_figure("fp64_pipe_active_pct")
+        cpu = None
+        if world == 1 and not a.no_cpu:
+            from oracle import oracle as O
+            threads = O.max_threads()
+            v, t = cpu_baseline(a.cpu_sample_log2, a.cpu_steps, a.solver, threads)
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": "2^%d-cell sample of the same basin, %d steps (%.1f s), OpenMP C restatement of the "
+                             "reference step" % (a.cpu_sample_log2, a.cpu_steps, t)}
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "cells": n,
+                       "solver": a.solver, "boundary": "outflow", "segment_cells": tiling[0],
+                       "block_threads": tiling[1], "l2": "inputs larger than L2 (2.1 GB state)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": roofline,
+            "fp64": {"dgemm_tflops_measured": fp64, "fp64_pipe_active_pct_ncu": fp64_util,
+                     "note": "the step is FP64-issue bound on GB300; see the ncu summary in profiles/"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": a.steps,
+            "clocks": clk,
+            "sim": {"time": sim_time, "dt": dt},
+        }
+        print(json.dumps(out))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+    return run_gpu(a, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

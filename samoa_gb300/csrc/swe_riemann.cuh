@@ -238,14 +238,18 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         fw[2][1] = ((huR * vR - huL * vL) - fw[2][0]) - fw[2][2];
     }
     // eliminate ghost fluxes of a wall (multiplication by 0 keeps the sign of zero)
-    if (wall_l || wall_r) {
-        int w0 = wall_l ? 0 : 1;
-        for (int w = w0; w < w0 + 2; ++w) {
-            sw[w] = sw[w] * 0.0;
-            fw[0][w] = fw[0][w] * 0.0;
-            fw[1][w] = fw[1][w] * 0.0;
-            fw[2][w] = fw[2][w] * 0.0;
-        }
+    auto zero_wave = [&](const int w) {
+        sw[w] = sw[w] * 0.0;
+        fw[0][w] = fw[0][w] * 0.0;
+        fw[1][w] = fw[1][w] * 0.0;
+        fw[2][w] = fw[2][w] * 0.0;
+    };
+    if (wall_l) {
+        zero_wave(0);
+        zero_wave(1);
+    } else if (wall_r) {
+        zero_wave(1);
+        zero_wave(2);
     }
 #pragma unroll
     for (int e = 0; e < 3; ++e) {

@@ -74,53 +74,84 @@ def parabolic_bowl(log2_cells=14, seed=2, solver="aug_riemann", amplitude=0.5, s
     return Scenario("parabolic_bowl", _grid(mesh, cfg, h, b), cfg, 500)
 
 
-def _hash2(ix, iy, seed):
-    v = (ix.astype(np.uint64) * np.uint64(0x9E3779B97F4A7C15)) ^ (iy.astype(np.uint64) * np.uint64(0xC2B2AE3D27D4EB4F))
-    v ^= np.uint64(seed) * np.uint64(0x165667B19E3779F9)
-    v ^= v >> np.uint64(31)
-    v *= np.uint64(0xBF58476D1CE4E5B9)
-    v ^= v >> np.uint64(29)
-    return (v >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0) * 2.0 - 1.0
-
-
 def value_noise(x, y, seed, octaves=5, base=8.0, persistence=0.5):
-    """Seeded lattice value noise in [-1, 1] with smooth-step interpolation, summed over octaves."""
+    """Seeded lattice value noise in [-1, 1], smooth-step interpolated, summed over
+    octaves (frequency doubling, amplitude times ``persistence``). x, y in [-0.5, 0.5]."""
+    rng = np.random.default_rng(seed)
     out = np.zeros_like(x)
     amp, freq, norm = 1.0, base, 0.0
-    with np.errstate(over="ignore"):
-        for o in range(octaves):
-            fx, fy = x * freq, y * freq
-            ix, iy = np.floor(fx), np.floor(fy)
-            tx, ty = fx - ix, fy - iy
-            ix = ix.astype(np.int64) + (1 << 20)
-            iy = iy.astype(np.int64) + (1 << 20)
-            sx, sy = tx * tx * (3 - 2 * tx), ty * ty * (3 - 2 * ty)
-            s = seed * 1000 + o
-            v00, v10 = _hash2(ix, iy, s), _hash2(ix + 1, iy, s)
-            v01, v11 = _hash2(ix, iy + 1, s), _hash2(ix + 1, iy + 1, s)
-            out += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sy) + (v01 * (1 - sx) + v11 * sx) * sy)
-            norm += amp
-            amp *= persistence
-            freq *= 2.0
+    for _ in range(octaves):
+        k = int(freq) + 3
+        table = rng.uniform(-1.0, 1.0, (k, k))
+        fx = (x + 0.5) * freq
+        fy = (y + 0.5) * freq
+        ix = np.clip(np.floor(fx).astype(np.int64), 0, k - 2)
+        iy = np.clip(np.floor(fy).astype(np.int64), 0, k - 2)
+        tx = fx - ix
+        ty = fy - iy
+        sx = tx * tx * (3.0 - 2.0 * tx)
+        sy = ty * ty * (3.0 - 2.0 * ty)
+        flat = table.ravel()
+        base_i = ix * k + iy
+        v00, v10 = flat[base_i], flat[base_i + k]
+        v01, v11 = flat[base_i + 1], flat[base_i + k + 1]
+        a = v00 + sx * (v10 - v00)
+        b = v01 + sx * (v11 - v01)
+        out += amp * (a + sy * (b - a))
+        norm += amp
+        amp *= persistence
+        freq *= 2.0
+    out /= norm
+    return out
+
+
+def _value_noise_torch(u, v, seed, octaves=5, base=8.0, persistence=0.5):
+    """value_noise() evaluated with torch (multi-threaded on the CPU, or on a GPU)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    out = torch.zeros_like(u)
+    amp, freq, norm = 1.0, base, 0.0
+    for _ in range(octaves):
+        k = int(freq) + 3
+        flat = torch.as_tensor(rng.uniform(-1.0, 1.0, (k, k)).ravel(), dtype=u.dtype, device=u.device)
+        fx = (u + 0.5) * freq
+        fy = (v + 0.5) * freq
+        ix = torch.clamp(torch.floor(fx), 0, k - 2)
+        iy = torch.clamp(torch.floor(fy), 0, k - 2)
+        tx, ty = fx - ix, fy - iy
+        sx = tx * tx * (3.0 - 2.0 * tx)
+        sy = ty * ty * (3.0 - 2.0 * ty)
+        bi = (ix * k + iy).long()
+        v00, v10, v01, v11 = flat[bi], flat[bi + k], flat[bi + 1], flat[bi + k + 1]
+        a = v00 + sx * (v10 - v00)
+        b = v01 + sx * (v11 - v01)
+        out += amp * (a + sy * (b - a))
+        norm += amp
+        amp *= persistence
+        freq *= 2.0
     return out / norm
 
 
-def ocean_basin(log2_cells=26, seed=3, solver="fwave", steps=200, mesh=None, scaling=1.0e6):
+def ocean_basin(log2_cells=26, seed=3, solver="fwave", steps=200, mesh=None, scaling=1.0e6, device="cpu"):
     """Synthetic ocean basin: tanh shelf from a -4000 m abyssal plain to a -50 m
     shelf plus 200 m of 5-octave seeded value noise, a Gaussian uplift of 2 m
-    with sigma 2 % of the domain width at a seeded centre; f-wave, outflow."""
+    with sigma 2 % of the domain width at a seeded centre; f-wave, outflow.
+    The fields are evaluated with torch on ``device`` (the mesh can have 2^26 cells)."""
+    import torch
     d = log2_cells - 1
     cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=0.01, scaling=scaling,
                  offset=(-0.5 * scaling, -0.5 * scaling), i_min_depth=d, i_max_depth=d)
     mesh = mesh or uniform_mesh(d)
-    u = mesh.centroids[:, 0] - 0.5
-    v = mesh.centroids[:, 1] - 0.5
+    cen = torch.from_numpy(mesh.centroids).to(device)
+    u = cen[:, 0] - 0.5
+    v = cen[:, 1] - 0.5
     rng = np.random.default_rng(seed)
-    x0, y0 = rng.uniform(-0.25, 0.1, 2)
-    b = -4000.0 + 3950.0 * 0.5 * (1.0 + np.tanh((u - 0.25) / 0.05)) + 200.0 * value_noise(u, v, seed)
-    b = np.minimum(b, -20.0)  # keep the shelf under water
-    eta = 2.0 * np.exp(-((u - x0) ** 2 + (v - y0) ** 2) / (2 * 0.02 * 0.02))
-    h = b + (eta - b)  # surface elevation eta over the bathymetry
+    x0, y0 = (float(t) for t in rng.uniform(-0.25, 0.1, 2))
+    b = -4000.0 + 3950.0 * 0.5 * (1.0 + torch.tanh((u - 0.25) / 0.05)) + 200.0 * _value_noise_torch(u, v, seed)
+    b = torch.clamp(b, max=-20.0)  # keep the shelf under water
+    eta = 2.0 * torch.exp(-((u - x0) ** 2 + (v - y0) ** 2) / (2 * 0.02 * 0.02))
+    h = eta.cpu().numpy()
+    b = b.cpu().numpy()
     return Scenario("ocean_basin", _grid(mesh, cfg, h, b), cfg, steps)
 
 
@@ -131,6 +162,6 @@ def lake_at_rest(log2_cells=10, solver="fwave", seed=7, mesh=None):
                  offset=(-0.5, -0.5), i_min_depth=0, i_max_depth=d + 1)
     mesh = mesh or uniform_mesh(d)
     x, y = _world(mesh, cfg)
-    b = -5.0 + 2.0 * value_noise(x + 0.5, y + 0.5, seed, octaves=3)
+    b = -5.0 + 2.0 * value_noise(x, y, seed, octaves=3)
     h = np.zeros(mesh.n_cells)
     return Scenario("lake_at_rest", _grid(mesh, cfg, h, b), cfg, 10)

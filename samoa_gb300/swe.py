@@ -256,14 +256,20 @@ def initial_dt(mesh: Mesh, h, hu, hv, b, courant):
     courant * min(volume / (sum(edge sizes) * max wave speed)), with the unscaled
     cell geometry the reference uses there."""
     from .geometry import leg_sizes, volumes
-    d = mesh.depth.astype(np.int64)
     leg = leg_sizes()
-    vol = volumes()[d]
-    edges = (leg[d + 1] + leg[d]) + leg[d + 1]
-    depth = h - b
-    wet = depth > 0.0
-    with np.errstate(divide="ignore", invalid="ignore"):
-        speed = np.where(wet, np.sqrt(G * depth) + np.sqrt((hu * hu + hv * hv) / (depth * depth)), 0.0)
-        dt = vol / (edges * speed)
-    dt = np.where(np.isnan(dt), np.inf, dt)
-    return courant * min(float(np.min(dt)), np.finfo(np.float64).max)
+    vols = volumes()
+    best = np.finfo(np.float64).max
+    for dd in np.unique(mesh.depth):
+        sel = mesh.depth == dd
+        dd = int(dd)
+        edges = (leg[dd + 1] + leg[dd]) + leg[dd + 1]
+        depth = h[sel] - b[sel]
+        wet = depth > 0.0
+        if not wet.any():
+            continue
+        dw = depth[wet]
+        speed = np.sqrt(G * dw) + np.sqrt((hu[sel][wet] ** 2 + hv[sel][wet] ** 2) / (dw * dw))
+        smax = float(speed.max())
+        if smax > 0.0:
+            best = min(best, vols[dd] / (edges * smax))
+    return courant * best
