@@ -136,8 +136,9 @@ int swe_synchronize(swe_ctx* ctx);
 /* Message of the last failure on this thread (always NUL-terminated). */
 int swe_last_error(char* buf, size_t n);
 
-/* Kernel tuning: cells per segment (even, 64..2048) and threads per block
- * (multiple of 32, 64..1024); 0 keeps the current value. A mesh upload or
+/* Kernel tuning: cells per segment (even, 64..1536; 16 doubles of shared
+ * memory per cell) and threads per block (multiple of 32, 64..256); 0 keeps
+ * the current value. A mesh upload or
  * this call rebuilds the segment task lists. */
 int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
 int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads);

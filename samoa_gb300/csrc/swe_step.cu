@@ -604,8 +604,8 @@ int swe_set_params(swe_ctx* c, const swe_params* p) {
 
 int swe_set_tiling(swe_ctx* c, int32_t seg_cells, int32_t block_threads) {
     if (!c) return set_error(SWE_E_INVALID, "null context");
-    if (seg_cells && (seg_cells < 64 || seg_cells > 2048 || (seg_cells & 1)))
-        return set_error(SWE_E_INVALID, "segment_cells %d: need an even value in 64..2048", seg_cells);
+    if (seg_cells && (seg_cells < 64 || seg_cells > 1536 || (seg_cells & 1)))
+        return set_error(SWE_E_INVALID, "segment_cells %d: need an even value in 64..1536", seg_cells);
     if (block_threads && (block_threads < 64 || block_threads > 256 || (block_threads & 31)))
         return set_error(SWE_E_INVALID, "block_threads %d: need a multiple of 32 in 64..256", block_threads);
     if (seg_cells) c->seg_cells = seg_cells;
