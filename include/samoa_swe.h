@@ -136,7 +136,7 @@ int swe_synchronize(swe_ctx* ctx);
 /* Message of the last failure on this thread (always NUL-terminated). */
 int swe_last_error(char* buf, size_t n);
 
-/* Kernel tuning: cells per segment (even, 64..1536; 16 doubles of shared
+/* Kernel tuning: cells per segment (even, 64..1536; 18 doubles of shared
  * memory per cell) and threads per block (multiple of 32, 64..256); 0 keeps
  * the current value. A mesh upload or
  * this call rebuilds the segment task lists. */
@@ -153,6 +153,34 @@ int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads)
 int swe_mesh_uniform(int32_t depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
                      int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell,
                      int8_t* bnd_local, double* centroids);
+
+/* ---- ensembles: many independent instances stepped together ------------ */
+/* An ensemble is a context with n_instances meshes that advance together, one
+ * kernel launch per time step for all of them, each instance with its own
+ * parameters, time and dt. No reference counterpart: sam(oa)^2 runs one
+ * scenario per process. Arrays are concatenated in instance order; cell
+ * indices in edge_cells / bnd_cell are local to their instance. State arrays
+ * (swe_state_upload/download) and flags are concatenated the same way
+ * (sum of n_cells entries). All instances must use the same solver. */
+int swe_ensemble_mesh_upload(swe_ctx* ctx, int64_t n_instances, const int64_t* n_cells, const int64_t* n_edges,
+                             const int64_t* n_bnd, const int8_t* depth, const int8_t* plotter,
+                             const int64_t* edge_cells, const int8_t* edge_local, const int64_t* bnd_cell,
+                             const int8_t* bnd_local);
+int swe_ensemble_set_params(swe_ctx* ctx, const swe_params* params /* [n_instances] */);
+int swe_ensemble_set_time(swe_ctx* ctx, const double* time, const double* dt);
+int swe_ensemble_get_time(swe_ctx* ctx, double* time, double* dt, double* dt_new);
+int swe_ensemble_get_refinements(swe_ctx* ctx, int8_t* flags, int64_t* n_refinements /* [n_instances] */);
+
+/* Run n_steps time steps as one CUDA graph: the first call with a given
+ * n_steps captures the launches, later calls replay the graph. No reference
+ * counterpart (the reference loop is host-driven, src/SWE/SWE.f90:380-429). */
+int swe_traverse_graph(swe_ctx* ctx, int64_t n_steps);
+
+/* Freeze the time-step sequence: the k-th step after this call uses
+ * dts[k * n_instances + i] for instance i instead of the CFL dt (for adjoint
+ * and finite-difference runs, where dt must not depend on the state);
+ * n_steps = 0 clears it. No reference counterpart. */
+int swe_set_dt_sequence(swe_ctx* ctx, int64_t n_steps, const double* dts);
 
 /* Check a mesh in the swe_mesh_upload layout on the host without a context
  * (same checks as the upload): 0 if valid, SWE_E_INVALID with a message otherwise. */

@@ -1,0 +1,285 @@
+"""FP64 torch restatement of the SWE step for the reference gradient (test infrastructure only).
+
+A vectorised, differentiable copy of the oracle's Jacobi-form step for the
+f-wave solver (src/geoclaw/riemannsolvers.f:446-500 inside
+c_bind_geoclaw_solver_dp, src/geoclaw/c_bind_riemannsolvers.f90:16-176; cell
+update src/SWE/SWE_euler_timestep.f90:257-355) on the C-ABI mesh layout. Its
+forward values equal the C oracle's bit for bit (tests check this); its
+gradient through torch.autograd, with the dt sequence frozen and every branch
+(wet/dry, wave-speed signs, min/max) differentiated on the side taken, is the
+FP64 CPU reference for the GPU's hand-written discrete adjoint.
+
+Only the f-wave solver with OUTFLOW, SLIP or NOSLIP walls is restated here;
+wall reconstruction at wet/dry edges (the riemanntype branch) is covered: its
+condition is evaluated like the solver does and its value changes are
+differentiated.
+"""
+import math
+
+import numpy as np
+import torch
+
+G = 9.80665
+
+
+class _ExactSqrt(torch.autograd.Function):
+    """Correctly rounded square root (numpy's IEEE sqrt): torch's vectorised CPU
+    sqrt is not correctly rounded on every build, and the restatement has to
+    match the oracle bit for bit."""
+
+    @staticmethod
+    def forward(ctx, x):
+        y = torch.from_numpy(np.sqrt(x.detach().cpu().numpy())).to(x.device)
+        ctx.save_for_backward(y)
+        return y
+
+    @staticmethod
+    def backward(ctx, gy):
+        (y,) = ctx.saved_tensors
+        safe = torch.where(y > 0, y, torch.ones_like(y))
+        return torch.where(y > 0, gy * 0.5 / safe, torch.zeros_like(gy))
+
+
+def _sqrt(x):
+    return _ExactSqrt.apply(x)
+
+
+def _where(c, a, b):
+    return torch.where(c, a, b)
+
+
+def _dmn(a, b):
+    return torch.where(a < b, a, b)
+
+
+def _dmx(a, b):
+    return torch.where(a > b, a, b)
+
+
+def _riemann_structure_hstar(hL, hR, uL, uR, drytol):
+    """hm of riemanntype (src/geoclaw/riemannsolvers.f:507-618), values only (it
+    decides the wall branch; no derivative flows through the condition)."""
+    g = G
+    hL, hR, uL, uR = (x.detach() for x in (hL, hR, uL, uR))
+    h_min = _dmn(hR, hL)
+    h_max = _dmx(hR, hL)
+    delu = uR - uL
+    safe = lambda x: torch.where(x > 0, x, torch.ones_like(x))
+    F_min = delu + 2.0 * (_sqrt(g * h_min) - _sqrt(g * h_max))
+    F_max = delu + (h_max - h_min) * _sqrt(((0.5 * g) * (h_max + h_min)) / safe(h_max * h_min))
+    t = _dmx(torch.zeros_like(delu), -delu + 2.0 * (_sqrt(g * hL) + _sqrt(g * hR)))
+    hm_rare = (1.0 / (16.0 * g)) * (t * t)
+    h0 = h_max
+    gL = _sqrt((0.5 * g) * (1.0 / safe(h0) + 1.0 / safe(hL)))
+    gR = _sqrt((0.5 * g) * (1.0 / safe(h0) + 1.0 / safe(hR)))
+    F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR
+    dfdh = ((gL - (g * (h0 - hL)) / ((4.0 * (h0 * h0)) * gL)) + gR) - (g * (h0 - hR)) / ((4.0 * (h0 * h0)) * gR)
+    slope = (2.0 * _sqrt(h0)) * dfdh
+    tt = _sqrt(h0) - F0 / torch.where(slope != 0, slope, torch.ones_like(slope))
+    hm_shock = tt * tt
+    h0 = h_min
+    F0b = (delu + 2.0 * (_sqrt(g * h0) - _sqrt(g * h_max))) + (h0 - h_min) * _sqrt(
+        (0.5 * g) * (1.0 / safe(h0) + 1.0 / safe(h_min)))
+    den = h_max - h_min
+    slope_b = (F_max - F0b) / torch.where(den != 0, den, torch.ones_like(den))
+    hm_mix = h0 - F0b / torch.where(slope_b != 0, slope_b, torch.ones_like(slope_b))
+    hm = torch.where(F_min > 0.0, hm_rare, torch.where(F_max <= 0.0, hm_shock, hm_mix))
+    return torch.where(h_min <= drytol, torch.zeros_like(hm), hm)
+
+
+def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol):
+    """compute_geoclaw_flux with the f-wave solver, vectorised over edges.
+    Returns the left and right net updates (h, hu, hv) in world coordinates."""
+    g = G
+    zero = torch.zeros_like(hsL)
+    one = torch.ones_like(hsL)
+    pL1 = n1 * pxL + n2 * pyL
+    pL2 = -n2 * pxL + n1 * pyL
+    pR1 = n1 * pxR + n2 * pyR
+    pR2 = -n2 * pxR + n1 * pyR
+    hL = hsL - bL
+    hR = hsR - bR
+    active = ~((hL <= drytol) & (hR <= drytol))
+    wetR = hR > drytol
+    wetL = hL > drytol
+    hRs = _where(wetR, hR, one)
+    hLs = _where(wetL, hL, one)
+    uR = _where(wetR, pR1 / hRs, zero)
+    vR = _where(wetR, pR2 / hRs, zero)
+    huR = _where(wetR, pR1, zero)
+    hvR = _where(wetR, pR2, zero)
+    hR = _where(wetR, hR, zero)
+    uL = _where(wetL, pL1 / hLs, zero)
+    vL = _where(wetL, pL2 / hLs, zero)
+    huL = _where(wetL, pL1, zero)
+    hvL = _where(wetL, pL2, zero)
+    hL = _where(wetL, hL, zero)
+    # wet/dry walls (c_bind_riemannsolvers.f90:87-115)
+    rdry = ~wetR
+    ldry = (~rdry) & (~wetL)
+    hst_r = _riemann_structure_hstar(hL, hL, uL, -uL, drytol)
+    wall_r = rdry & (_dmx(hL.detach(), hst_r) + bL < bR)
+    lower_r = rdry & (~wall_r) & (hL + bL < bR)
+    hst_l = _riemann_structure_hstar(hR, hR, -uR, uR, drytol)
+    wall_l = ldry & (_dmx(hR.detach(), hst_l) + bR < bL)
+    lower_l = ldry & (~wall_l) & (hR + bR < bL)
+    hR_, huR_, bR_, uR_, vR_ = (_where(wall_r, hL, hR), _where(wall_r, -huL, huR), _where(wall_r, bL, bR),
+                                _where(wall_r, -uL, uR), _where(wall_r, vL, vR))
+    bR_ = _where(lower_r, hL + bL, bR_)
+    hL_, huL_, bL_, uL_, vL_ = (_where(wall_l, hR, hL), _where(wall_l, -huR, huL), _where(wall_l, bR, bL),
+                                _where(wall_l, -uR, uL), _where(wall_l, vR, vL))
+    bL_ = _where(lower_l, hR + bR, bL_)
+    hR, huR, bR, uR, vR = hR_, huR_, bR_, uR_, vR_
+    hL, huL, bL, uL, vL = hL_, huL_, bL_, uL_, vL_
+
+    delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) +
+              (((0.5 * g) * (((bR + hR) - bL) - hL)) * (hR + hL))) - (((0.5 * g) * (hR + hL)) * (bR - bL))
+    sq_in_L = g * hL
+    sq_in_R = g * hR
+    sqL = _sqrt(_where(sq_in_L > 0, sq_in_L, one)) * (sq_in_L > 0)
+    sqR = _sqrt(_where(sq_in_R > 0, sq_in_R, one)) * (sq_in_R > 0)
+    sL = uL - sqL
+    sR = uR + sqR
+    den = sqR + sqL
+    uhat = (sqL * uL + sqR * uR) / _where(den > 0, den, one)
+    ch_in = (g * 0.5) * (hR + hL)
+    chat = _sqrt(_where(ch_in > 0, ch_in, one)) * (ch_in > 0)
+    sE1 = _dmn(sL, uhat - chat)
+    sE2 = _dmx(sR, uhat + chat)
+    delhu = huR - huL
+    delb = bR - bL
+    deldelphi = -(((g * 0.5) * (hR + hL)) * delb)
+    dpd = delphi - deldelphi
+    ds = sE2 - sE1
+    ds = _where(ds != 0, ds, one)
+    beta1 = (sE2 * delhu - dpd) / ds
+    beta2 = (dpd - sE1 * delhu) / ds
+    sw = [sE1, 0.5 * (sE1 + sE2), sE2]
+    fw = [[beta1, zero, beta2], [beta1 * sE1, zero, beta2 * sE2], [beta1 * vL, None, beta2 * vR]]
+    fw[2][1] = ((huR * vR - huL * vL) - fw[2][0]) - fw[2][2]
+    walls = [wall_l, wall_l | wall_r, wall_r]
+    for w in range(3):
+        sw[w] = _where(walls[w], sw[w] * 0.0, sw[w])
+        for e in range(3):
+            fw[e][w] = _where(walls[w], fw[e][w] * 0.0, fw[e][w])
+    netL = [zero, zero, zero]
+    netR = [zero, zero, zero]
+    for e in range(3):
+        for w in range(3):
+            neg, pos = sw[w] < 0.0, sw[w] > 0.0
+            f = fw[e][w]
+            netL[e] = _where(neg, netL[e] + f, _where(pos, netL[e], netL[e] + 0.5 * f))
+            netR[e] = _where(pos, netR[e] + f, _where(neg, netR[e], netR[e] + 0.5 * f))
+    netL = [_where(active, x, zero) for x in netL]
+    netR = [_where(active, x, zero) for x in netR]
+    fL = (netL[0], netL[1] * n1 + netL[2] * -n2, netL[1] * n2 + netL[2] * n1)
+    fR = (netR[0], netR[1] * n1 + netR[2] * -n2, netR[1] * n2 + netR[2] * n1)
+    return fL, fR
+
+
+class TorchStep:
+    """The step on a fixed mesh (C-ABI layout), f-wave, differentiable.
+
+    Edges are oriented by the step parity exactly like the GPU kernel; ``step``
+    applies one Euler step with a given dt to (h, hu, hv) for bathymetry b.
+    """
+
+    def __init__(self, mesh, scaling=1.0, drytol=0.01, bc="outflow"):
+        from oracle import oracle as O
+        self.n = mesh.n_cells
+        self.drytol = drytol
+        self.bc = bc
+        ec = torch.as_tensor(np.asarray(mesh.edge_cells, np.int64))
+        el = torch.as_tensor(np.asarray(mesh.edge_local, np.int64)) - 1
+        self.ea, self.eb = ec[:, 0], ec[:, 1]
+        self.la, self.lb = el[:, 0], el[:, 1]
+        self.bcell = torch.as_tensor(np.asarray(mesh.bnd_cell, np.int64))
+        self.bloc = torch.as_tensor(np.asarray(mesh.bnd_local, np.int64)) - 1
+        table = np.zeros((17, 3, 2))
+        for p in range(-8, 9):
+            if p:
+                for e in range(3):
+                    table[p + 8, e] = O.normal(p, e + 1)
+        table = torch.as_tensor(table)
+        pl = torch.as_tensor(np.asarray(mesh.plotter, np.int64)) + 8
+        self.nA = table[pl[self.ea], self.la]
+        self.nB = table[pl[self.eb], self.lb]
+        self.nBnd = table[pl[self.bcell], self.bloc]
+        d = torch.as_tensor(np.asarray(mesh.depth, np.int64))
+        leg = torch.as_tensor([O.leg_size(i) for i in range(-1, 61)], dtype=torch.float64)
+        vol = torch.as_tensor([O.cell_volume(i) for i in range(0, 61)], dtype=torch.float64)
+        self.leg = scaling * leg[d + 1]
+        self.hyp = scaling * leg[d]
+        self.vol = (scaling * scaling) * vol[d]
+
+    def step(self, h, hu, hv, b, dt, parity):
+        n = self.n
+        odd = parity & 1
+        if odd:
+            L, R, iL, iR, nn = self.eb, self.ea, self.lb, self.la, self.nB
+        else:
+            L, R, iL, iR, nn = self.ea, self.eb, self.la, self.lb, self.nA
+        fL, fR = fwave_flux(nn[:, 0], nn[:, 1], h[L], hu[L], hv[L], b[L], h[R], hu[R], hv[R], b[R], self.drytol)
+        c = self.bcell
+        n1, n2 = self.nBnd[:, 0], self.nBnd[:, 1]
+        gp1, gp2 = hu[c], hv[c]
+        if self.bc == "slip":
+            dd = hu[c] * n1 + hv[c] * n2
+            gp1, gp2 = hu[c] - dd * n1, hv[c] - dd * n2
+        elif self.bc == "noslip":
+            gp1, gp2 = -hu[c], -hv[c]
+        fB, _ = fwave_flux(n1, n2, h[c], hu[c], hv[c], b[c], h[c], gp1, gp2, b[c], self.drytol)
+        # slot values [cell, local edge]
+        slots = []
+        for q in range(3):
+            s = torch.zeros(n, 3, dtype=h.dtype)
+            s = s.index_put((L, iL), fL[q], accumulate=True)
+            s = s.index_put((R, iR), fR[q], accumulate=True)
+            s = s.index_put((c, self.bloc), fB[q], accumulate=True)
+            slots.append(s)
+        k0, k2 = (2, 0) if odd else (0, 2)
+        sc = -dt / self.vol
+        d = []
+        for q in range(3):
+            s = slots[q]
+            d.append((self.leg * s[:, k0] + self.hyp * s[:, 1]) + self.leg * s[:, k2])
+        dh, dp1, dp2 = (sc * x for x in d)
+        wet_fix = (h < b + self.drytol) & (dh > 0.0)
+        h1 = _where(wet_fix, b + self.drytol, h)
+        p1 = _where(wet_fix, torch.zeros_like(hu), hu)
+        p2 = _where(wet_fix, torch.zeros_like(hv), hv)
+        h1 = h1 + dh
+        p1 = p1 + dp1
+        p2 = p2 + dp2
+        dry = h1 < b + self.drytol
+        h1 = _where(dry, _dmn(b, torch.zeros_like(b)), h1)
+        p1 = _where(dry, torch.zeros_like(p1), p1)
+        p2 = _where(dry, torch.zeros_like(p2), p2)
+        return h1, p1, p2
+
+
+def gauge_objective_and_grad(tstep, h0, hu0, hv0, b, dts, gauges, obs, parity0=0, need_grad=True):
+    """J = sum_t sum_g (h_t[gauge] - obs[t, g])^2 over len(dts) steps and its
+    gradient with respect to h0 and b, by reverse accumulation one step at a
+    time (states kept on the host; each step re-run under autograd)."""
+    states = [(h0, hu0, hv0)]
+    J = 0.0
+    with torch.no_grad():
+        for t, dt in enumerate(dts):
+            h, hu, hv = tstep.step(*states[-1], b, float(dt), parity0 + t)
+            states.append((h, hu, hv))
+            J += float(((h[gauges] - obs[t]) ** 2).sum())
+    if not need_grad:
+        return J, None, None
+    lam = [torch.zeros_like(h0), torch.zeros_like(h0), torch.zeros_like(h0)]
+    gb = torch.zeros_like(b)
+    for t in range(len(dts) - 1, -1, -1):
+        hT = states[t + 1][0]
+        lam[0] = lam[0].index_add(0, gauges, 2.0 * (hT[gauges] - obs[t]))
+        x = [s.clone().requires_grad_(True) for s in states[t]]
+        bb = b.clone().requires_grad_(True)
+        out = tstep.step(*x, bb, float(dts[t]), parity0 + t)
+        grads = torch.autograd.grad(out, x + [bb], grad_outputs=lam, allow_unused=True)
+        lam = [g if g is not None else torch.zeros_like(h0) for g in grads[:3]]
+        gb = gb + (grads[3] if grads[3] is not None else 0.0)
+    return J, lam[0], gb

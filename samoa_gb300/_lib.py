@@ -18,7 +18,9 @@ EXPORTS = [
     "swe_create", "swe_destroy", "swe_set_stream", "swe_set_params", "swe_mesh_upload", "swe_state_upload",
     "swe_state_download", "swe_state_device", "swe_set_time", "swe_get_time", "swe_traverse",
     "swe_get_refinements", "swe_get_step_count", "swe_synchronize", "swe_last_error", "swe_set_tiling",
-    "swe_get_tiling", "swe_mesh_uniform", "swe_mesh_validate", "swe_riemann_batch",
+    "swe_get_tiling", "swe_mesh_uniform", "swe_mesh_validate", "swe_riemann_batch", "swe_ensemble_mesh_upload",
+    "swe_ensemble_set_params", "swe_ensemble_set_time", "swe_ensemble_get_time", "swe_ensemble_get_refinements",
+    "swe_traverse_graph", "swe_set_dt_sequence",
 ]
 
 
@@ -68,6 +70,13 @@ def load():
         "swe_mesh_uniform": [i32, P, P, P, P, P, P, P, P, P, P],
         "swe_mesh_validate": [i64, P, P, i64, P, P, i64, P, P],
         "swe_riemann_batch": [i32, i64, P, P, P, dbl, P, P],
+        "swe_ensemble_mesh_upload": [P, i64, P, P, P, P, P, P, P, P, P],
+        "swe_ensemble_set_params": [P, P],
+        "swe_ensemble_set_time": [P, P, P],
+        "swe_ensemble_get_time": [P, P, P, P],
+        "swe_ensemble_get_refinements": [P, P, P],
+        "swe_traverse_graph": [P, i64],
+        "swe_set_dt_sequence": [P, i64, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

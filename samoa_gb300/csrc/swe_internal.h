@@ -26,19 +26,30 @@ inline uint32_t pack_meta(int la, int lb, int pa, int pb, bool bnd) {
            ((uint32_t)(bnd ? 1 : 0) << 14);
 }
 
-// Device-resident scalars of a context. The step kernel reads step and dt,
-// reduces into dt_acc / refine_acc, and the last block to finish advances time,
-// dt and step, so many steps run back to back without the host.
-struct DevScalars {
+// Per-instance parameters on the device (the cfg fields the step reads,
+// src/Config.f90:30-121, plus the depth range present in the instance's mesh).
+struct InstParams {
+    double drytol, courant, scaling, thr_refine, thr_coarsen, max_time, tout;
+    int32_t min_depth, max_depth, dmin, ndepth, bc, pad;
+};
+
+// Per-instance scalars on the device. The step kernel reads dt, reduces into
+// dt_acc / refine_acc, and the last CTA to finish advances time and dt, so
+// many steps run back to back without the host.
+struct InstScalars {
     double time;                    // grid%r_time
     double dt;                      // grid%r_dt for the next step
     double dt_new;                  // min(volume / sum(len * speed)) of the last step
     unsigned long long dt_acc;      // bits of the running minimum (non-negative doubles order as integers)
     unsigned long long refine_acc;  // refinements issued in the running step
     unsigned long long n_refine;    // refinements issued in the last step
-    unsigned int done;              // blocks finished in the running step
-    unsigned int error;             // nonzero: a kernel saw a bad index or a wait ran out
-    long long step;                 // steps since the mesh upload (parity = traversal direction)
+};
+
+struct GlobalScalars {
+    unsigned int done;       // CTAs finished in the running step
+    unsigned int error;      // nonzero: a kernel saw a bad index or a wait ran out
+    long long step;          // steps since the mesh upload (parity = traversal direction)
+    long long dt_seq_base;   // step at which the frozen dt sequence starts
 };
 
 // Mesh as ingested from the C ABI (validated, a < b on inner edges).
@@ -58,7 +69,13 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
 int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
                 const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
                 const int8_t* bnd_local);
-int build_tasks(const HostMesh& m, int32_t seg_cells, std::vector<int64_t>& seg_ptr, std::vector<Task>& tasks);
+// Segment descriptor: cells [c0, c0 + cn) of instance `inst`.
+struct alignas(16) SegInfo {
+    int32_t c0, cn, inst, pad;
+};
+
+int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t seg_cells, std::vector<int64_t>& seg_ptr,
+                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks);
 
 // Geometry tables restating src/SFC_data_types.f90:509-700 (host side, exact).
 void geometry_tables(double leg[kMaxDepth + 2], double vol[kMaxDepth + 1], double normal[17][3][2]);

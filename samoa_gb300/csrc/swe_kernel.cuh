@@ -1,0 +1,392 @@
+// The fused SWE time-step kernel (sm_103a).
+//
+// One launch = one explicit Euler time step of every instance of the context
+// (one instance for the plain step, many for an ensemble) of
+// t_swe_euler_timestep_traversal (src/SWE/SWE_euler_timestep.f90). Cells are
+// cut into segments of consecutive cells of the space-filling curve; a
+// segment never spans two instances. A persistent grid of CTAs walks the
+// segments; per segment:
+//   1. stage h, hu, hv, b into shared memory with 1-D TMA bulk copies
+//      (cp.async.bulk, completion on an mbarrier with a bounded wait), then
+//      the depth h - b and sqrt(g * depth) once per cell;
+//   2. evaluate each edge task once: the Riemann solver with the first-touched
+//      cell as the left side writes left/right updates into per-(cell, local
+//      edge) slots in shared memory, each slot written by one task, no atomics;
+//      an edge between two segments is evaluated by both CTAs, each keeping
+//      its own side, so no CTA waits for another;
+//   3. update each cell from its three slots in local edge index order, clamp
+//      wet/dry, write the other state buffer, set the refinement flag, fold
+//      volume / sum(len * speed) into a running minimum;
+// at an instance change and at the end the CTA reduces the minimum with warp
+// shuffles and folds it into the instance with one atomic; the last CTA to
+// finish advances every instance's time and dt and the step counter.
+// The reference's traversal direction alternates every step
+// (src/SFC_generic_traversal_ringbuffer.f90:420): on odd steps the
+// higher-numbered cell of an edge is touched first and the two leg updates are
+// summed in the other order.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "swe_internal.h"
+#include "swe_riemann.cuh"
+
+namespace swe {
+
+__constant__ double c_leg[kMaxDepth + 2];  // sqrt(0.5)**i at [i + 1], i = -1..60
+__constant__ double c_vol[kMaxDepth + 1];  // 0.5**(i + 1)
+__constant__ double c_normal[17][3][2];    // [plotter + 8][local edge][x, y]
+
+struct StepArgs {
+    double* h[2];
+    double* hu[2];
+    double* hv[2];
+    const double* b;
+    const int8_t* depth;
+    int8_t* flags;
+    const int4* tasks;
+    const long long* seg_ptr;
+    const int4* seg_info;      // {first cell, cells, instance, 0}
+    const InstParams* ip;
+    InstScalars* is;
+    GlobalScalars* gs;
+    const double* dt_seq;      // frozen dt sequence [k * n_inst + inst] or null
+    long long dt_seq_len;      // steps in the sequence
+    int32_t n_seg, n_inst, seg_cells, max_ndepth, n_cells_total;
+    int32_t use_tma;
+};
+
+constexpr int kWaitLimit = 1 << 24;  // polls of an mbarrier before a kernel gives up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 1-D bulk copy global -> this CTA's shared memory; addresses 16-byte aligned,
+// size a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = dmn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ long long warp_sum(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// dt of step `step` for instance `inst`: the frozen sequence if one is set,
+// else grid%r_dt clamped as in pre_traversal_grid_op (src/SWE/SWE_euler_timestep.f90:89-109)
+__device__ __forceinline__ double step_dt(const StepArgs& A, const InstParams& P, int inst, long long k) {
+    if (A.dt_seq && k >= 0 && k < A.dt_seq_len) return A.dt_seq[k * A.n_inst + inst];
+    double dt = A.is[inst].dt;
+    if (P.max_time > 0.0) dt = dmn(P.max_time, dt);
+    if (P.tout > 0.0) dt = dmn(P.tout, dt);
+    return dt;
+}
+
+// Block-wide reduction of (dtmin, nref) into instance `inst`; all threads call it.
+__device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, double& dtmin, long long& nref,
+                                               double* red_min, long long* red_sum) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double m = warp_min(dtmin);
+    long long s = warp_sum(nref);
+    if (lane == 0) {
+        red_min[warp] = m;
+        red_sum[warp] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        m = lane < nw ? red_min[lane] : DBL_MAX;
+        s = lane < nw ? red_sum[lane] : 0;
+        m = warp_min(m);
+        s = warp_sum(s);
+        if (lane == 0) {
+            // non-negative doubles order like their bit patterns
+            atomicMin(&A.is[inst].dt_acc, (unsigned long long)__double_as_longlong(m));
+            if (s) atomicAdd(&A.is[inst].refine_acc, (unsigned long long)s);
+        }
+    }
+    __syncthreads();
+    dtmin = DBL_MAX;
+    nref = 0;
+}
+
+template <int SOLVER>
+__global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int T = A.seg_cells;
+    double* sh_h = reinterpret_cast<double*>(smem_raw);
+    double* sh_hu = sh_h + T;
+    double* sh_hv = sh_hu + T;
+    double* sh_b = sh_hv + T;
+    double* sh_d = sh_b + T;        // depth h - b
+    double* sh_sq = sh_d + T;       // sqrt(g * depth) where the cell is wet
+    double* upd = sh_sq + T;        // [4 quantities][3 local edges][T cells]
+    double* tab_leg = upd + 12 * T; // per depth of the current instance
+    double* tab_hyp = tab_leg + A.max_ndepth;
+    double* tab_vol = tab_hyp + A.max_ndepth;
+    double* tab_ndv = tab_vol + A.max_ndepth;  // -dt / volume
+    __shared__ uint64_t bar;
+    __shared__ double red_min[32];
+    __shared__ long long red_sum[32];
+    __shared__ unsigned int s_error;
+    __shared__ int s_last;
+
+    const int tid = threadIdx.x;
+    const long long step = A.gs->step;
+    const long long kseq = step - A.gs->dt_seq_base;
+    const int odd = (int)(step & 1);
+    const double* hin = A.h[odd];
+    const double* huin = A.hu[odd];
+    const double* hvin = A.hv[odd];
+    double* hout = A.h[odd ^ 1];
+    double* huout = A.hu[odd ^ 1];
+    double* hvout = A.hv[odd ^ 1];
+
+    if (tid == 0) {
+        s_error = 0;
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    double dtmin = DBL_MAX;  // r_dt_new = huge(1.0) (pre_traversal_op, :133-140)
+    long long nref = 0;
+    uint32_t phase = 0;
+    int cur = -1;
+    InstParams P;
+
+    for (int seg = blockIdx.x; seg < A.n_seg; seg += gridDim.x) {
+        const int4 si = __ldg(&A.seg_info[seg]);
+        const int c0 = si.x, cn = si.y, inst = si.z;
+        if (inst != cur) {  // uniform across the CTA
+            if (cur >= 0) flush_instance(A, cur, dtmin, nref, red_min, red_sum);
+            P = A.ip[inst];
+            const double dt = step_dt(A, P, inst, kseq);
+            for (int i = tid; i < P.ndepth; i += blockDim.x) {
+                const int d = P.dmin + i;
+                const double vol = (P.scaling * P.scaling) * c_vol[d];
+                tab_leg[i] = P.scaling * c_leg[d + 1];
+                tab_hyp[i] = P.scaling * c_leg[d];
+                tab_vol[i] = vol;
+                tab_ndv[i] = -dt / vol;
+            }
+            cur = inst;
+        }
+        // ---- 1. stage the segment's state
+        const int cbulk = A.use_tma ? (cn & ~1) : 0;  // 16-byte multiple (c0 is even)
+        if (cbulk > 0 && tid == 0) {
+            fence_proxy_async();
+            const uint32_t bytes = (uint32_t)cbulk * 8u;
+            mbar_arrive_expect_tx(&bar, 4u * bytes);
+            bulk_g2s(sh_h, hin + c0, bytes, &bar);
+            bulk_g2s(sh_hu, huin + c0, bytes, &bar);
+            bulk_g2s(sh_hv, hvin + c0, bytes, &bar);
+            bulk_g2s(sh_b, A.b + c0, bytes, &bar);
+        }
+        for (int i = cbulk + tid; i < cn; i += blockDim.x) {
+            sh_h[i] = hin[c0 + i];
+            sh_hu[i] = huin[c0 + i];
+            sh_hv[i] = hvin[c0 + i];
+            sh_b[i] = A.b[c0 + i];
+        }
+        if (cbulk > 0) {
+            int polls = 0;
+            while (!mbar_try_wait(&bar, phase)) {
+                if (++polls > kWaitLimit) {
+                    s_error = 2u;
+                    break;
+                }
+            }
+            phase ^= 1u;
+        }
+        __syncthreads();
+        if (s_error) break;
+        for (int i = tid; i < cn; i += blockDim.x) {
+            double d, sq;
+            depth_terms(State{sh_h[i], 0.0, 0.0, sh_b[i]}, P.drytol, d, sq);
+            sh_d[i] = d;
+            sh_sq[i] = sq;
+        }
+        __syncthreads();
+
+        // ---- 2. edge tasks (skeleton_scalar_op / bnd_skeleton_scalar_op, :196-255)
+        const long long t0 = A.seg_ptr[seg], t1 = A.seg_ptr[seg + 1];
+        for (long long t = t0 + tid; t < t1; t += blockDim.x) {
+            const int4 tk = __ldg(&A.tasks[t]);
+            const uint32_t meta = (uint32_t)tk.z;
+            const bool bnd = (meta >> 14) & 1u;
+            int L, R, iL, iR, pL;
+            if (bnd || !odd) {
+                L = tk.x; iL = meta & 3u; pL = (meta >> 4) & 31u;
+                R = tk.y; iR = (meta >> 2) & 3u;
+            } else {
+                L = tk.y; iL = (meta >> 2) & 3u; pL = (meta >> 9) & 31u;
+                R = tk.x; iR = meta & 3u;
+            }
+            if ((unsigned)L >= (unsigned)A.n_cells_total || (!bnd && (unsigned)R >= (unsigned)A.n_cells_total) ||
+                iL > 2 || iR > 2 || pL > 16) {
+                atomicOr(&s_error, 1u);
+                continue;
+            }
+            const double n1 = c_normal[pL][iL][0], n2 = c_normal[pL][iL][1];
+            const int sl = L - c0, sr = R - c0;
+            const bool lin = (unsigned)sl < (unsigned)cn;
+            const bool rin = !bnd && (unsigned)sr < (unsigned)cn;
+            State QL, QR;
+            double dL, dR, sqL, sqR;
+            if (lin) {
+                QL = State{sh_h[sl], sh_hu[sl], sh_hv[sl], sh_b[sl]};
+                dL = sh_d[sl];
+                sqL = sh_sq[sl];
+            } else {
+                QL = State{hin[L], huin[L], hvin[L], A.b[L]};
+                depth_terms(QL, P.drytol, dL, sqL);
+            }
+            if (bnd) {  // the ghost has the cell's h and b
+                if (P.bc == BC_SLIP) QR = boundary_ghost<BC_SLIP>(n1, n2, QL);
+                else if (P.bc == BC_NOSLIP) QR = boundary_ghost<BC_NOSLIP>(n1, n2, QL);
+                else QR = QL;
+                dR = dL;
+                sqR = sqL;
+            } else if (rin) {
+                QR = State{sh_h[sr], sh_hu[sr], sh_hv[sr], sh_b[sr]};
+                dR = sh_d[sr];
+                sqR = sh_sq[sr];
+            } else {
+                QR = State{hin[R], huin[R], hvin[R], A.b[R]};
+                depth_terms(QR, P.drytol, dR, sqR);
+            }
+            Update fL, fR;
+            edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, P.drytol, fL, fR);
+            if (lin) {
+                upd[(0 * 3 + iL) * T + sl] = fL.h;
+                upd[(1 * 3 + iL) * T + sl] = fL.p1;
+                upd[(2 * 3 + iL) * T + sl] = fL.p2;
+                upd[(3 * 3 + iL) * T + sl] = fL.s;
+            }
+            if (rin) {
+                upd[(0 * 3 + iR) * T + sr] = fR.h;
+                upd[(1 * 3 + iR) * T + sr] = fR.p1;
+                upd[(2 * 3 + iR) * T + sr] = fR.p2;
+                upd[(3 * 3 + iR) * T + sr] = fR.s;
+            }
+        }
+        __syncthreads();
+
+        // ---- 3. cell updates: cell_update_op + volume_op (src/SWE/SWE_euler_timestep.f90:257-355)
+        const int k0 = odd ? 2 : 0, k2 = odd ? 0 : 2;
+        for (int i = tid; i < cn; i += blockDim.x) {
+            const int c = c0 + i;
+            const int d = A.depth[c];
+            const int di = d - P.dmin;
+            const double leg = tab_leg[di], hyp = tab_hyp[di], vol = tab_vol[di], ndv = tab_ndv[di];
+            double dh = z0(leg * upd[(0 * 3 + k0) * T + i]) + hyp * upd[(0 * 3 + 1) * T + i];
+            dh = dh + leg * upd[(0 * 3 + k2) * T + i];
+            double dp1 = z0(leg * upd[(1 * 3 + k0) * T + i]) + hyp * upd[(1 * 3 + 1) * T + i];
+            dp1 = dp1 + leg * upd[(1 * 3 + k2) * T + i];
+            double dp2 = z0(leg * upd[(2 * 3 + k0) * T + i]) + hyp * upd[(2 * 3 + 1) * T + i];
+            dp2 = dp2 + leg * upd[(2 * 3 + k2) * T + i];
+            double ds = z0(leg * upd[(3 * 3 + k0) * T + i]) + hyp * upd[(3 * 3 + 1) * T + i];
+            ds = ds + leg * upd[(3 * 3 + k2) * T + i];
+            int8_t f = 0;
+            const double nrm = fabs(dh);
+            if (d < P.max_depth && nrm > P.thr_refine) {
+                f = 1;
+                ++nref;
+            } else if (d > P.min_depth && nrm < P.thr_coarsen) {
+                f = -1;
+            }
+            dtmin = dmn(dtmin, vol / ds);
+            dh = ndv * dh;
+            dp1 = ndv * dp1;
+            dp2 = ndv * dp2;
+            double h = sh_h[i], p1 = sh_hu[i], p2 = sh_hv[i];
+            const double b = sh_b[i];
+            if (h < b + P.drytol && dh > 0.0) {  // flooded land starts at the dry tolerance, at rest
+                h = b + P.drytol;
+                p1 = 0.0;
+                p2 = 0.0;
+            }
+            h = h + dh;
+            p1 = p1 + dp1;
+            p2 = p2 + dp2;
+            if (h < b + P.drytol) {  // dried out: surface to min(b, 0), at rest
+                h = dmn(b, 0.0);
+                p1 = 0.0;
+                p2 = 0.0;
+            }
+            hout[c] = h;
+            huout[c] = p1;
+            hvout[c] = p2;
+            A.flags[c] = f;
+        }
+        __syncthreads();
+    }
+
+    // ---- 4. reductions and the last-CTA finalisation (post_traversal_grid_op, :111-131)
+    if (cur >= 0) flush_instance(A, cur, dtmin, nref, red_min, red_sum);
+    if (tid == 0) {
+        if (s_error) atomicOr(&A.gs->error, s_error);
+        __threadfence();
+        s_last = atomicAdd(&A.gs->done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int i = tid; i < A.n_inst; i += blockDim.x) {
+            const InstParams Q = A.ip[i];
+            const double dt = step_dt(A, Q, i, kseq);
+            InstScalars* S = &A.is[i];
+            const double dtn = __longlong_as_double((long long)atomicAdd(&S->dt_acc, 0ull));
+            S->time = S->time + dt;
+            S->dt_new = dtn;
+            S->dt = Q.courant * dtn;
+            S->n_refine = atomicExch(&S->refine_acc, 0ull);
+            S->dt_acc = (unsigned long long)__double_as_longlong(DBL_MAX);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            A.gs->done = 0;
+            A.gs->step = step + 1;
+            __threadfence();
+        }
+    }
+}
+
+}  // namespace swe

@@ -4,6 +4,7 @@
 // reads. Both run once per remesh, not per step.
 #include "swe_internal.h"
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -168,43 +169,59 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
     return SWE_OK;
 }
 
-// Per-segment edge tasks. An inner edge with both cells in one segment is one
-// task there; an edge between two segments is a task in both (each keeps its
-// own side, so no segment waits for another). A boundary edge is a task in its
-// cell's segment.
-int build_tasks(const HostMesh& m, int32_t T, std::vector<int64_t>& seg_ptr, std::vector<Task>& tasks) {
+// Per-segment edge tasks of one instance whose cells start at `offset` in the
+// context's arrays; appended to seg_ptr / seg_info / tasks. An inner edge with
+// both cells in one segment is one task there; an edge between two segments is
+// a task in both (each keeps its own side, so no segment waits for another). A
+// boundary edge is a task in its cell's segment. Boundary tasks come first in a
+// segment, then inner edges in stream (first-touch) order.
+int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std::vector<int64_t>& seg_ptr,
+                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks) {
     const int64_t n = m.n_cells;
     const int64_t nseg = (n + T - 1) / T;
-    seg_ptr.assign((size_t)nseg + 1, 0);
+    if (seg_ptr.empty()) seg_ptr.push_back(0);
+    const size_t s0 = seg_info.size();
+    std::vector<int64_t> count((size_t)nseg + 1, 0);
     for (int64_t e = 0; e < m.n_edges; ++e) {
-        int64_t sa = m.ea[e] / T, sb = m.eb[e] / T;
-        seg_ptr[sa + 1]++;
-        if (sb != sa) seg_ptr[sb + 1]++;
+        int64_t sa = m.ea[(size_t)e] / T, sb = m.eb[(size_t)e] / T;
+        count[(size_t)sa + 1]++;
+        if (sb != sa) count[(size_t)sb + 1]++;
     }
-    for (int64_t j = 0; j < m.n_bnd; ++j) seg_ptr[m.bc[j] / T + 1]++;
-    for (int64_t s = 0; s < nseg; ++s) seg_ptr[s + 1] += seg_ptr[s];
-    tasks.resize((size_t)seg_ptr[nseg]);
-    std::vector<int64_t> fill(seg_ptr.begin(), seg_ptr.end() - 1);
-    // boundary edges first inside each segment, then inner edges in stream order
+    for (int64_t j = 0; j < m.n_bnd; ++j) count[(size_t)(m.bc[(size_t)j] / T) + 1]++;
+    for (int64_t s = 0; s < nseg; ++s) count[(size_t)s + 1] += count[(size_t)s];
+    const int64_t base = seg_ptr.back();
+    for (int64_t s = 0; s < nseg; ++s) {
+        seg_ptr.push_back(base + count[(size_t)s + 1]);
+        SegInfo si;
+        si.c0 = (int32_t)(offset + s * T);
+        si.cn = (int32_t)std::min<int64_t>(T, n - s * T);
+        si.inst = inst;
+        si.pad = 0;
+        seg_info.push_back(si);
+    }
+    (void)s0;
+    tasks.resize((size_t)(base + count[(size_t)nseg]));
+    std::vector<int64_t> fill(count.begin(), count.end() - 1);
+    for (auto& f : fill) f += base;
     for (int64_t j = 0; j < m.n_bnd; ++j) {
-        int64_t c = m.bc[j];
+        int64_t c = m.bc[(size_t)j];
         Task t;
-        t.a = (int32_t)c;
+        t.a = (int32_t)(offset + c);
         t.b = -1;
-        t.meta = pack_meta(m.bl[j] - 1, 0, m.plotter[c], 1, true);
+        t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true);
         t.pad = 0;
-        tasks[(size_t)fill[c / T]++] = t;
+        tasks[(size_t)fill[(size_t)(c / T)]++] = t;
     }
     for (int64_t e = 0; e < m.n_edges; ++e) {
-        int64_t a = m.ea[e], b = m.eb[e];
+        int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
         Task t;
-        t.a = (int32_t)a;
-        t.b = (int32_t)b;
-        t.meta = pack_meta(m.la[e] - 1, m.lb[e] - 1, m.plotter[a], m.plotter[b], false);
+        t.a = (int32_t)(offset + a);
+        t.b = (int32_t)(offset + b);
+        t.meta = pack_meta(m.la[(size_t)e] - 1, m.lb[(size_t)e] - 1, m.plotter[(size_t)a], m.plotter[(size_t)b], false);
         t.pad = 0;
         int64_t sa = a / T, sb = b / T;
-        tasks[(size_t)fill[sa]++] = t;
-        if (sb != sa) tasks[(size_t)fill[sb]++] = t;
+        tasks[(size_t)fill[(size_t)sa]++] = t;
+        if (sb != sa) tasks[(size_t)fill[(size_t)sb]++] = t;
     }
     return SWE_OK;
 }

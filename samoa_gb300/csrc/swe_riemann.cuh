@@ -96,7 +96,8 @@ __device__ __forceinline__ double det3(double a00, double a01, double a02, doubl
 // states after the Cramer solve never reach the outputs.
 __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
                                          double uL, double uR, double vL, double vR, double delphi, double sE1,
-                                         double sE2, double drytol, double sw[3], double fw[3][3]) {
+                                         double sE2, double sqL, double sqR, double drytol, double sw[3],
+                                         double fw[3][3]) {
     const double g = kG;
     double delh = hR - hL;
     double delhu = huR - huL;
@@ -127,8 +128,8 @@ __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, doubl
     if (dmn(fabs(sE1), fabs(sE2)) < ct) sonic = true;
     if (sE1 < 0.0 && s1m > 0.0) sonic = true;
     if (sE2 > 0.0 && s2m < 0.0) sonic = true;
-    if ((uL + sqrt(g * hL)) * (uR + sqrt(g * hR)) < 0.0) sonic = true;
-    if ((uL - sqrt(g * hL)) * (uR - sqrt(g * hR)) < 0.0) sonic = true;
+    if ((uL + sqL) * (uR + sqR) < 0.0) sonic = true;  // sqrt(g * h) of the fixed-up depths
+    if ((uL - sqL) * (uR - sqR) < 0.0) sonic = true;
 
     double deldelh = sonic ? -delb : ((delb * g) * hbar) / s1s2bar;
     if (sE1 < -ct && sE2 > ct) {
@@ -166,10 +167,13 @@ __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, doubl
 // (src/geoclaw/c_bind_riemannsolvers.f90:16-176) with the f-wave
 // (src/geoclaw/riemannsolvers.f:446-500) or augmented solver. netL/netR are
 // the left/right net updates of (h, hu, hv) in the edge frame.
+// sqL0 / sqR0 are sqrt(g * depth) of the two cells, computed once per cell by the
+// caller; they are used only where the reference evaluates sqrt(g * h) on an
+// unmodified wet depth (the same operands, so the same bits).
 template <int SOLVER>
 __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL, double huR, double hvL,
-                                               double hvR, double bL, double bR, double drytol, double netL[3],
-                                               double netR[3], double& maxspeed) {
+                                               double hvR, double bL, double bR, double sqL0, double sqR0,
+                                               double drytol, double netL[3], double netR[3], double& maxspeed) {
     const double g = kG;
     netL[0] = netL[1] = netL[2] = 0.0;
     netR[0] = netR[1] = netR[2] = 0.0;
@@ -213,7 +217,11 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     double delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) +
                      (((0.5 * g) * (((bR + hR) - bL) - hL)) * (hR + hL))) -
                     (((0.5 * g) * (hR + hL)) * (bR - bL));
-    double sqL = sqrt(g * hL), sqR = sqrt(g * hR);
+    // sqrt(g * h) after the wet/dry fix-ups: a wet side keeps its depth, a dry one
+    // has depth 0, and a wall mirrors the wet side's depth
+    const bool wetL = hL > drytol || wall_l, wetR = hR > drytol || wall_r;
+    double sqL = wetL ? (wall_l ? sqR0 : sqL0) : 0.0;
+    double sqR = wetR ? (wall_r ? sqL0 : sqR0) : 0.0;
     double sL = uL - sqL;
     double sR = uR + sqR;
     double uhat = (sqL * uL + sqR * uR) / (sqR + sqL);
@@ -223,7 +231,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
 
     double sw[3], fw[3][3];
     if (SOLVER == AUG_RIEMANN) {
-        riemann_aug(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, drytol, sw, fw);
+        riemann_aug(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR, drytol, sw, fw);
     } else {
         double delhu = huR - huL;
         double delb = bR - bL;
@@ -251,17 +259,29 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         zero_wave(1);
         zero_wave(2);
     }
+    // net updates: each accumulator starts at +0 and takes its waves in wave order;
+    // +0 + x is z0(x), and the f-wave's wave 2 carries exact +0 in h and hu,
+    // which leaves an accumulator unchanged (it is never -0)
+    bool tL[3] = {false, false, false}, tR[3] = {false, false, false};
+    auto acc = [](double& a, bool& t, double c) {
+        a = t ? a + c : z0(c);
+        t = true;
+    };
 #pragma unroll
-    for (int e = 0; e < 3; ++e) {
+    for (int w = 0; w < 3; ++w) {
+        const bool neg = sw[w] < 0.0, pos = sw[w] > 0.0;
 #pragma unroll
-        for (int w = 0; w < 3; ++w) {
-            if (sw[w] < 0.0) {
-                netL[e] = netL[e] + fw[e][w];
-            } else if (sw[w] > 0.0) {
-                netR[e] = netR[e] + fw[e][w];
+        for (int e = 0; e < 3; ++e) {
+            if (SOLVER != AUG_RIEMANN && w == 1 && e < 2) continue;
+            const double f = fw[e][w];
+            if (neg) {
+                acc(netL[e], tL[e], f);
+            } else if (pos) {
+                acc(netR[e], tR[e], f);
             } else {
-                netL[e] = netL[e] + 0.5 * fw[e][w];
-                netR[e] = netR[e] + 0.5 * fw[e][w];
+                const double hf = 0.5 * f;
+                acc(netL[e], tL[e], hf);
+                acc(netR[e], tR[e], hf);
             }
         }
     }
@@ -273,15 +293,16 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
 
 // compute_geoclaw_flux, src/SWE/SWE_euler_timestep.f90:449-481
 template <int SOLVER>
-__device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR,
-                                             double drytol, Update& fL, Update& fR) {
+__device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR, double dL,
+                                             double dR, double sqL, double sqR, double drytol, Update& fL,
+                                             Update& fR) {
     // T = [[n1, n2], [-n2, n1]]; p_edge = T p
     double pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
     double pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
     double pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
     double pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
     double netL[3], netR[3], ms;
-    geoclaw_solver<SOLVER>(QL.h - QL.b, QR.h - QR.b, pL1, pR1, pL2, pR2, QL.b, QR.b, drytol, netL, netR, ms);
+    geoclaw_solver<SOLVER>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, drytol, netL, netR, ms);
     // p = net(2:3) T
     fL.h = netL[0];
     fL.p1 = z0(netL[1] * n1) + netL[2] * -n2;
@@ -299,11 +320,10 @@ __device__ __forceinline__ double normal_velocity(double n1, double n2, double p
 
 // compute_lf_flux, src/SWE/SWE_euler_timestep.f90:359-446
 template <int SOLVER>
-__device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, const State& QR, double drytol,
-                                        Update& fL, Update& fR) {
+__device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, const State& QR, double dL,
+                                        double dR, double drytol, Update& fL, Update& fR) {
     const double g = kG;
     if (SOLVER == LF_BATH || SOLVER == LLF_BATH) {
-        double dL = QL.h - QL.b, dR = QR.h - QR.b;
         if (dL < drytol || dR < drytol) {
             fL = Update{0.0, 0.0, 0.0, 0.0};
             fR = Update{0.0, 0.0, 0.0, 0.0};
@@ -344,7 +364,8 @@ __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, c
         fR.p1 = fR.p1 + src * n1;
         fR.p2 = fR.p2 + src * n2;
     } else {
-        double dL = QL.h - 0.0, dR = QR.h - 0.0;
+        dL = QL.h - 0.0;
+        dR = QR.h - 0.0;
         double hL = dmx(dL, 0.0), hR = dmx(dR, 0.0);
         double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
         double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
@@ -362,13 +383,21 @@ __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, c
     }
 }
 
+// One edge: dL/dR are the depths h - b of the two states, sqL/sqR their
+// sqrt(g * depth) (only read for depths above the dry tolerance).
 template <int SOLVER>
-__device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL, const State& QR, double drytol,
-                                          Update& fL, Update& fR) {
+__device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL, const State& QR, double dL,
+                                          double dR, double sqL, double sqR, double drytol, Update& fL, Update& fR) {
     if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
-        geoclaw_flux<SOLVER>(n1, n2, QL, QR, drytol, fL, fR);
+        geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, drytol, fL, fR);
     else
-        lf_flux<SOLVER>(n1, n2, QL, QR, drytol, fL, fR);
+        lf_flux<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, fL, fR);
+}
+
+// depth and sqrt(g * depth) of a state, as the edge code needs them
+__device__ __forceinline__ void depth_terms(const State& Q, double drytol, double& d, double& sq) {
+    d = Q.h - Q.b;
+    sq = d > drytol ? sqrt(kG * d) : 0.0;
 }
 
 // Ghost state of bnd_skeleton_scalar_op, src/SWE/SWE_euler_timestep.f90:231-255.

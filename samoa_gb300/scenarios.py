@@ -165,3 +165,45 @@ def lake_at_rest(log2_cells=10, solver="fwave", seed=7, mesh=None):
     b = -5.0 + 2.0 * value_noise(x, y, seed, octaves=3)
     h = np.zeros(mesh.n_cells)
     return Scenario("lake_at_rest", _grid(mesh, cfg, h, b), cfg, 10)
+
+
+@dataclass
+class Ensemble:
+    name: str
+    meshes: list
+    grids: list
+    cfgs: list
+    steps: int
+
+
+def bowl_ensemble(n_instances=512, seed=4, log2_range=(12, 20), solver="fwave", steps=1000, device="cpu"):
+    """Ensemble of independent parabolic-bowl instances: uniform meshes of 2^k
+    cells with k uniform in ``log2_range`` (4k..1M cells), the bowl bathymetry,
+    a Gaussian surface bump per instance with amplitude U[0.5, 3] m, sigma
+    U[0.03, 0.08] and a seeded centre; f-wave, CFL 0.5, each with its own dt."""
+    import torch
+    rng = np.random.default_rng(seed)
+    ks = rng.integers(log2_range[0], log2_range[1] + 1, n_instances)
+    amps = rng.uniform(0.5, 3.0, n_instances)
+    sigmas = rng.uniform(0.03, 0.08, n_instances)
+    centres = rng.uniform(-0.15, 0.15, (n_instances, 2))
+    cache = {}
+    meshes, grids, cfgs = [], [], []
+    for i in range(n_instances):
+        k = int(ks[i])
+        if k not in cache:
+            cache[k] = uniform_mesh(k - 1)
+        mesh = cache[k]
+        cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.5, dry_tolerance=1e-3, scaling=1.0,
+                     offset=(-0.5, -0.5), i_min_depth=k - 1, i_max_depth=k - 1)
+        cen = torch.from_numpy(mesh.centroids).to(device)
+        x = cen[:, 0] - 0.5
+        y = cen[:, 1] - 0.5
+        b = -10.0 * (1.0 - (x * x + y * y) / 0.16)
+        eta = amps[i] * torch.exp(-((x - centres[i, 0]) ** 2 + (y - centres[i, 1]) ** 2) / (2 * sigmas[i] ** 2))
+        h = torch.where(b < eta, eta, b)
+        g = _grid(mesh, cfg, h.cpu().numpy(), b.cpu().numpy())
+        meshes.append(mesh)
+        grids.append(g)
+        cfgs.append(cfg)
+    return Ensemble("bowl_ensemble", meshes, grids, cfgs, steps)

@@ -192,6 +192,63 @@ class SweContext:
     def synchronize(self):
         _lib.check(self.L.swe_synchronize(self.ptr))
 
+    def traverse_graph(self, n_steps):
+        """n_steps steps as one CUDA graph (captured on first use, replayed afterwards)."""
+        _lib.check(self.L.swe_traverse_graph(self.ptr, int(n_steps)))
+
+    def set_dt_sequence(self, dts):
+        """Freeze the dt of the next len(dts) steps (shape (steps,) or (steps, n_instances)); None clears."""
+        if dts is None or len(dts) == 0:
+            _lib.check(self.L.swe_set_dt_sequence(self.ptr, 0, None))
+            return
+        a = np.ascontiguousarray(dts, np.float64)
+        _lib.check(self.L.swe_set_dt_sequence(self.ptr, a.shape[0], _p(a)))
+
+
+class SweEnsemble(SweContext):
+    """Many independent SWE instances stepped together: one kernel launch per
+    time step for all instances, each with its own parameters and dt."""
+
+    def upload_meshes(self, meshes):
+        nc = np.array([m.n_cells for m in meshes], np.int64)
+        ne = np.array([len(m.edge_cells) for m in meshes], np.int64)
+        nb = np.array([len(m.bnd_cell) for m in meshes], np.int64)
+        cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs), dt)
+        d = cat([m.depth for m in meshes], np.int8)
+        p = cat([m.plotter for m in meshes], np.int8)
+        ec = cat([m.edge_cells.reshape(-1, 2) for m in meshes], np.int64)
+        el = cat([m.edge_local.reshape(-1, 2) for m in meshes], np.int8)
+        bc = cat([m.bnd_cell for m in meshes], np.int64)
+        bl = cat([m.bnd_local for m in meshes], np.int8)
+        _lib.check(self.L.swe_ensemble_mesh_upload(self.ptr, len(meshes), _p(nc), _p(ne), _p(nb), _p(d), _p(p),
+                                                   _p(ec), _p(el), _p(bc), _p(bl)))
+        self.n_instances = len(meshes)
+        self.sizes = nc
+        self.n_cells = int(nc.sum())
+
+    def set_params_list(self, params):
+        arr = (_lib.SweParams * len(params))(*params)
+        _lib.check(self.L.swe_ensemble_set_params(self.ptr, arr))
+
+    def set_times(self, times, dts):
+        t = np.ascontiguousarray(times, np.float64)
+        d = np.ascontiguousarray(dts, np.float64)
+        _lib.check(self.L.swe_ensemble_set_time(self.ptr, _p(t), _p(d)))
+
+    def get_times(self):
+        t, d, dn = (np.empty(self.n_instances) for _ in range(3))
+        _lib.check(self.L.swe_ensemble_get_time(self.ptr, _p(t), _p(d), _p(dn)))
+        return t, d, dn
+
+    def refinements_all(self):
+        f = np.empty(self.n_cells, np.int8)
+        n = np.empty(self.n_instances, np.int64)
+        _lib.check(self.L.swe_ensemble_get_refinements(self.ptr, _p(f), _p(n)))
+        return f, n
+
+    def split(self, a):
+        return np.split(a, np.cumsum(self.sizes)[:-1])
+
 
 class SweEulerTimestepTraversal:
     """GPU drop-in for t_swe_euler_timestep_traversal (src/SWE/SWE_euler_timestep.f90).
