@@ -196,6 +196,32 @@ int swe_mesh_validate(int64_t n_cells, const int8_t* depth, const int8_t* plotte
 int swe_riemann_batch(int32_t solver, int64_t n, const double* normals, const double* q_left, const double* q_right,
                       double dry_tolerance, double* out_left, double* out_right);
 
+/* One time step on caller-owned device memory, allocating nothing. No
+ * counterpart in the reference. For callers that cannot allocate device memory
+ * at the point where they step (a host code whose device memory all comes from
+ * its own pool, or that steps where an allocation would synchronise the device):
+ * every argument after `params` is a device pointer the caller owns, in the
+ * layout of swe_mesh_upload / swe_state_upload; the step reads (h, hu, hv, b),
+ * writes (h_out, hu_out, hv_out) and the refinement flags (flags may be NULL),
+ * uses dt as given (no clamps), the traversal parity `parity` (0 = the given
+ * cell order, 1 = reversed, as on the odd steps after an upload), and writes
+ * min(volume / sum(len * speed)) to *dt_new and the refinement count to
+ * *n_refinements (-1 if an index was out of range), both device pointers.
+ * The work goes on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ * and the call returns without synchronising.
+ * Limits: n_cells <= 65,536. The scratch (edge updates and reduction
+ * accumulators, 6.3 MB) is one fixed array in device memory that every GPU which
+ * loads the library keeps until exit; all calls share it, so calls that overlap
+ * on the GPU (different streams, or without ordering) race. The first call on a
+ * device sets it up (cudaGetSymbolAddress, geometry tables, clearing the
+ * accumulators, one device synchronisation): make that first call before any
+ * stream capture. */
+int swe_step_noalloc(const swe_params* params, int64_t n_cells, const int8_t* depth, const int8_t* plotter,
+                     int64_t n_edges, const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd,
+                     const int64_t* bnd_cell, const int8_t* bnd_local, const double* h, const double* hu,
+                     const double* hv, const double* b, double* h_out, double* hu_out, double* hv_out, int8_t* flags,
+                     double dt, int32_t parity, double* dt_new, int64_t* n_refinements, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ EXPORTS = [
     "swe_get_refinements", "swe_get_step_count", "swe_synchronize", "swe_last_error", "swe_set_tiling",
     "swe_get_tiling", "swe_mesh_uniform", "swe_mesh_validate", "swe_riemann_batch", "swe_ensemble_mesh_upload",
     "swe_ensemble_set_params", "swe_ensemble_set_time", "swe_ensemble_get_time", "swe_ensemble_get_refinements",
-    "swe_traverse_graph", "swe_set_dt_sequence",
+    "swe_traverse_graph", "swe_set_dt_sequence", "swe_step_noalloc",
 ]
 
 
@@ -77,6 +77,7 @@ def load():
         "swe_ensemble_get_refinements": [P, P, P],
         "swe_traverse_graph": [P, i64],
         "swe_set_dt_sequence": [P, i64, P],
+        "swe_step_noalloc": [P, i64, P, P, i64, P, P, i64, P, P, P, P, P, P, P, P, P, P, dbl, i32, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

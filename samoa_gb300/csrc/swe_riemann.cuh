@@ -33,7 +33,7 @@ __device__ __forceinline__ double dmn(double a, double b) { return (a < b) ? a :
 __device__ __forceinline__ double dmx(double a, double b) { return (a > b) ? a : b; }
 
 // Riemann structure with one Newton step, src/geoclaw/riemannsolvers.f:507-618.
-__device__ __noinline__ void riemann_structure(double hL, double hR, double uL, double uR, double drytol,
+static __device__ __noinline__ void riemann_structure(double hL, double hR, double uL, double uR, double drytol,
                                                double& hm, double& s1m, double& s2m) {
     const double g = kG;
     double h_min = dmn(hR, hL);
@@ -94,7 +94,7 @@ __device__ __forceinline__ double det3(double a00, double a01, double a02, doubl
 // Augmented solver (George 2008) with maxiter = 1, src/geoclaw/riemannsolvers.f:2-258.
 // The entropy corrector is off in the source; with one iteration the star
 // states after the Cramer solve never reach the outputs.
-__device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
+static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
                                          double uL, double uR, double vL, double vR, double delphi, double sE1,
                                          double sE2, double sqL, double sqR, double drytol, double sw[3],
                                          double fw[3][3]) {
