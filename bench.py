@@ -46,8 +46,16 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--segment-cells", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
+    ap.add_argument("--arith", default="strict", choices=["strict", "fma"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ensemble-instances", type=int, default=512)
+    ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--adjoint-log2-cells", type=int, default=18)
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--adjoint-fd", type=int, default=16)
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -209,6 +217,114 @@ def fp64_dgemm_tflops(torch):
     return best
 
 
+def ensemble_compare(a, device):
+    """Batched ensemble (one launch per step for all instances, replayed as a
+    CUDA graph) against looping the plain step over the same instances (one
+    context per instance, all on one stream), same GPU, same steps."""
+    import torch
+
+    from samoa_gb300 import scenarios, swe
+    ens = scenarios.bowl_ensemble(n_instances=a.ensemble_instances, seed=4, device="cuda")
+    cells = int(sum(m.n_cells for m in ens.meshes))
+    K = a.ensemble_steps
+    stream = torch.cuda.Stream(device=device)
+    cat = lambda k: np.concatenate([getattr(g, k) for g in ens.grids])
+
+    batched = swe.SweEnsemble(device)
+    batched.upload_meshes(ens.meshes)
+    batched.set_params_list([c.params() for c in ens.cfgs])
+    batched.upload_state(cat("h"), cat("hu"), cat("hv"), cat("b"))
+    batched.set_times([0.0] * len(ens.grids), [g.r_dt for g in ens.grids])
+    batched.set_stream(stream.cuda_stream)
+    batched.traverse_graph(K)  # capture + warm-up
+    batched.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    batched.traverse_graph(K)
+    e1.record(stream)
+    e1.synchronize()
+    batched.synchronize()
+    t_batched = e0.elapsed_time(e1) * 1e-3
+    batched.close()
+
+    ctxs = []
+    for m, g, c in zip(ens.meshes, ens.grids, ens.cfgs):
+        x = swe.SweContext(device)
+        x.set_params(c.params())
+        x.upload_mesh(m)
+        x.upload_state(g.h, g.hu, g.hv, g.b)
+        x.set_time(0.0, g.r_dt)
+        x.set_stream(stream.cuda_stream)
+        ctxs.append(x)
+    for x in ctxs:
+        x.traverse(1)  # warm-up
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(K):
+        for x in ctxs:
+            x.traverse(1)
+    e1.record(stream)
+    e1.synchronize()
+    t_loop = e0.elapsed_time(e1) * 1e-3
+    for x in ctxs:
+        x.synchronize()
+        x.close()
+    v_b = cells * K / t_batched
+    v_l = cells * K / t_loop
+    return {"instances": len(ens.grids), "cells": cells, "steps": K, "batched": v_b, "looped": v_l,
+            "speedup": v_b / v_l, "unit": UNIT,
+            "note": "bowl ensemble, 2^12..2^20 cells per instance, f-wave, own dt per instance; batched = one "
+                    "launch per step for all instances replayed as a CUDA graph; looped = the plain step launched "
+                    "per instance on one stream"}
+
+
+def adjoint_compare(a, device):
+    """Gauge-misfit gradient through the adjoint against the forward run it
+    differentiates: 2^18 cells, 2,000 steps, 64 snapshots, f-wave, frozen dt;
+    the gradient is checked by central differences in seeded random directions."""
+    from samoa_gb300 import adjoint, scenarios
+    case = scenarios.adjoint_case(log2_cells=a.adjoint_log2_cells, steps=a.adjoint_steps, n_gauges=32, seed=5,
+                                  device=device)
+    P = adjoint.GaugeProblem(case["mesh"], case["params"], case["gauges"], case["obs"], case["dts"], snapshots=64,
+                             device=device)
+    try:
+        P.objective(case["h0"], case["b"], record=False)  # warm-up
+        t0 = time.perf_counter()
+        J = P.objective(case["h0"], case["b"], record=False)
+        t_fwd = time.perf_counter() - t0
+        P.stats = {"forward_steps": 0, "adjoint_steps": 0}
+        t0 = time.perf_counter()
+        J2, gh, gb = P.gradient(case["h0"], case["b"])
+        t_grad = time.perf_counter() - t0
+        stats = dict(P.stats)
+        gh, gb = gh.cpu().numpy(), gb.cpu().numpy()
+        rng = np.random.default_rng(16)
+        worst = 0.0
+        for k in range(a.adjoint_fd):
+            d = rng.normal(size=gh.shape)
+            if k % 2 == 0:
+                eps = 1e-6 * float(np.abs(case["h0"]).max())
+                Jp = P.objective(case["h0"] + eps * d, case["b"], record=False)
+                Jm = P.objective(case["h0"] - eps * d, case["b"], record=False)
+                ad = float(gh @ d)
+            else:
+                eps = 1e-6 * float(np.abs(case["b"]).max())
+                Jp = P.objective(case["h0"], case["b"] + eps * d, record=False)
+                Jm = P.objective(case["h0"], case["b"] - eps * d, record=False)
+                ad = float(gb @ d)
+            worst = max(worst, abs((Jp - Jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
+        t_step, t_adj = adjoint.time_steps(P, 50)
+    finally:
+        P.close()
+    n = case["mesh"].n_cells
+    return {"cells": n, "steps": a.adjoint_steps, "snapshots": 64, "J": J, "forward_s": t_fwd, "gradient_s": t_grad,
+            "gradient_over_forward": t_grad / t_fwd, "forward_steps_in_gradient": stats["forward_steps"],
+            "adjoint_steps": stats["adjoint_steps"], "fd_directions": a.adjoint_fd, "fd_max_rel_err": worst,
+            "forward_step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj, "adjoint_step_over_forward_step": t_adj / t_step,
+            "note": "gradient_s = forward run + checkpointed reverse sweep (recomputation included); J(h0, b) is "
+                    "the squared misfit at 32 gauges; dt frozen; the FD check uses the same frozen dts"}
+
+
 def run_gpu(a, rank, world, local):
     import torch
     import torch.distributed as dist
@@ -226,6 +342,7 @@ def run_gpu(a, rank, world, local):
     n = g.mesh.n_cells
     ctx = swe.SweContext(local)
     ctx.set_params(scn.cfg.params())
+    ctx.set_arith(a.arith)
     if a.segment_cells or a.block_threads:
         ctx.set_tiling(a.segment_cells, a.block_threads)
     ctx.upload_mesh(g.mesh)
@@ -311,19 +428,34 @@ def run_gpu(a, rank, world, local):
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": "2^%d-cell sample of the same basin, %d steps (%.1f s), OpenMP C restatement of the "
                              "reference step" % (a.cpu_sample_log2, a.cpu_steps, t)}
+        ensemble = None
+        if world == 1 and not a.no_ensemble:
+            try:
+                ensemble = ensemble_compare(a, local)
+            except Exception as exc:  # reported, never hides the headline number
+                ensemble = {"error": repr(exc)[:300]}
+        adj = None
+        if world == 1 and not a.no_adjoint:
+            try:
+                adj = adjoint_compare(a, local)
+            except Exception as exc:
+                adj = {"error": repr(exc)[:300]}
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "cells": n,
                        "solver": a.solver, "boundary": "outflow", "segment_cells": tiling[0],
-                       "block_threads": tiling[1], "l2": "inputs larger than L2 (2.1 GB state)",
+                       "block_threads": tiling[1], "arith": a.arith,
+                       "l2": "inputs larger than L2 (2.1 GB state)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline,
             "fp64": {"dgemm_tflops_measured": fp64, "fp64_pipe_active_pct_ncu": fp64_util,
                      "note": "the step is FP64-issue bound on GB300; see the ncu summary in profiles/"},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "ensemble": ensemble,
+            "adjoint": adj,
             "gpu_launches": a.steps,
             "clocks": clk,
             "sim": {"time": sim_time, "dt": dt},

@@ -141,6 +141,17 @@ int swe_last_error(char* buf, size_t n);
  * the current value. A mesh upload or
  * this call rebuilds the segment task lists. */
 int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
+
+/* Arithmetic of the step kernel. STRICT (the default): every FP64 operation
+ * rounded separately, in the reference's evaluation order, so results are bit
+ * identical to a strict-IEEE CPU evaluation of the reference step. FMA: the
+ * same kernel with multiply-adds fused by the compiler; faster on GB300's FP64
+ * pipe, results within a few ulps per step of STRICT (not bit identical). No
+ * reference counterpart (the reference's precision is a compile-time choice,
+ * SConstruct:272-278). Adjoint steps always use STRICT. */
+#define SWE_ARITH_STRICT 0
+#define SWE_ARITH_FMA 1
+int swe_set_arith(swe_ctx* ctx, int32_t mode);
 int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads);
 
 /* Uniform Sierpinski mesh of the unit square at reference depth `depth`
@@ -181,6 +192,40 @@ int swe_traverse_graph(swe_ctx* ctx, int64_t n_steps);
  * and finite-difference runs, where dt must not depend on the state);
  * n_steps = 0 clears it. No reference counterpart. */
 int swe_set_dt_sequence(swe_ctx* ctx, int64_t n_steps, const double* dts);
+
+/* ---- discrete adjoint (single-instance contexts, f-wave solver) ---------- */
+/* No reference counterpart: sam(oa)^2 has no adjoint. Cotangent buffers are
+ * device pointers with n_cells doubles each. */
+
+/* Copy the current state (h, hu, hv) to caller device buffers and return the
+ * step count (its parity is the traversal direction); restore sets the state
+ * and the step count back (time is not restored). For checkpointing. */
+int swe_snapshot_store(swe_ctx* ctx, double* h, double* hu, double* hv, int64_t* step);
+int swe_snapshot_restore(swe_ctx* ctx, const double* h, const double* hu, const double* hv, int64_t step);
+
+/* Surface elevation h of the current state at the given cells (device arrays;
+ * NaN for an index out of range), asynchronously: a gauge sampler on the
+ * device (the point output of src/SWE/SWE_point_output.f90:226-266 at order 0). */
+int swe_sample_gauges(swe_ctx* ctx, int64_t n_gauges, const int64_t* cells, double* out);
+
+/* Run n_steps steps like swe_traverse and record each step's wet/dry branches
+ * (per cell: bit 0 wetting fix, bit 1 drying clamp) at branch + i * stride
+ * for the i-th step (device buffer, stride >= n_cells). */
+int swe_traverse_branches(swe_ctx* ctx, int64_t n_steps, uint8_t* branch, int64_t stride);
+
+/* Undo the last step: valid right after a step, whose input state is still in
+ * the other state buffer; sets the step count back by one (time is kept). */
+int swe_step_back(swe_ctx* ctx);
+
+/* One reverse step. The context is at step t with state x_t. Given
+ * lam = dJ/dx_{t+1}, writes out = dJ/dx_t and adds dJ/db of step t to bbar,
+ * differentiating every branch on the side the forward step took; dt is the
+ * frozen value of swe_set_dt_sequence, which is required. `branch` holds the
+ * branches recorded when step t ran forward (swe_traverse_branches); with
+ * branch = NULL the step first runs forward itself to record them and the
+ * context is left at step t+1, else it stays at step t. */
+int swe_adjoint_step(swe_ctx* ctx, const uint8_t* branch, const double* lam_h, const double* lam_hu,
+                     const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar);
 
 /* Check a mesh in the swe_mesh_upload layout on the host without a context
  * (same checks as the upload): 0 if valid, SWE_E_INVALID with a message otherwise. */

@@ -20,7 +20,8 @@ EXPORTS = [
     "swe_get_refinements", "swe_get_step_count", "swe_synchronize", "swe_last_error", "swe_set_tiling",
     "swe_get_tiling", "swe_mesh_uniform", "swe_mesh_validate", "swe_riemann_batch", "swe_ensemble_mesh_upload",
     "swe_ensemble_set_params", "swe_ensemble_set_time", "swe_ensemble_get_time", "swe_ensemble_get_refinements",
-    "swe_traverse_graph", "swe_set_dt_sequence", "swe_step_noalloc",
+    "swe_traverse_graph", "swe_set_dt_sequence", "swe_step_noalloc", "swe_snapshot_store", "swe_snapshot_restore",
+    "swe_sample_gauges", "swe_adjoint_step", "swe_set_arith", "swe_traverse_branches", "swe_step_back",
 ]
 
 
@@ -78,6 +79,13 @@ def load():
         "swe_traverse_graph": [P, i64],
         "swe_set_dt_sequence": [P, i64, P],
         "swe_step_noalloc": [P, i64, P, P, i64, P, P, i64, P, P, P, P, P, P, P, P, P, P, dbl, i32, P, P, P],
+        "swe_snapshot_store": [P, P, P, P, P],
+        "swe_snapshot_restore": [P, P, P, P, i64],
+        "swe_sample_gauges": [P, i64, P, P],
+        "swe_adjoint_step": [P, P, P, P, P, P, P, P, P],
+        "swe_traverse_branches": [P, i64, P, i64],
+        "swe_step_back": [P],
+        "swe_set_arith": [P, i32],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -17,7 +17,9 @@ LIB = os.path.join(HERE, "libsamoa_swe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-O2,-fno-fast-math",
               "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["swe_step.cu", "swe_mesh.cpp", "swe_geometry.cpp", "swe_noalloc.cu"]
+SOURCES = ["swe_step.cu", "swe_mesh.cpp", "swe_geometry.cpp", "swe_noalloc.cu", "swe_step_fma.cu"]
+# the FMA-contraction variant of the step kernels (an opt-in arithmetic mode)
+FLAGS_OVERRIDE = {"swe_step_fma.cu": ["--fmad=true"]}
 
 
 def _nvcc():
@@ -35,7 +37,8 @@ def _deps():
 
 def _compile(src, extra):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+    flags = [f for f in NVCC_FLAGS if not (f.startswith("--fmad") and src in FLAGS_OVERRIDE)]
+    cmd = [_nvcc(), *ARCH, *flags, *FLAGS_OVERRIDE.get(src, []), *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     if src.endswith(".cpp"):
         cmd = [_nvcc(), "-x", "cu", *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     subprocess.check_call(cmd)

@@ -1,0 +1,437 @@
+// Discrete adjoint of the SWE step (f-wave solver), hand-written reverse mode.
+//
+// The step x' = F(x, b; dt) is differentiated on the branches its forward
+// evaluation takes (wet/dry fix-ups, wall reconstruction, the Einfeldt
+// min/max, the wave-speed signs that split the net updates, the cell's
+// wetting and drying clamps). dt is frozen (it enters as a constant), so the
+// CFL reduction and the wave speeds' magnitudes are not differentiated.
+//
+// Per edge, fwave_vjp re-evaluates the forward flux of geoclaw_flux<FWAVE>
+// (the same expressions, so the same branches as the forward step) and pulls
+// the cotangents of the two net updates back to (h, hu, hv, b) of both
+// cells. The reverse-step kernel mirrors the forward kernel: a CTA stages a
+// segment, evaluates each edge task's VJP once and writes each side's result
+// into a per-(cell, local edge) slot in shared memory (no atomics), then each
+// cell sums its slots and its own direct term.
+#pragma once
+
+#include "swe_kernel.cuh"
+
+namespace swe {
+
+struct Grad4 {
+    double h, hu, hv, b;
+};
+
+// VJP of the f-wave edge flux: given the cotangents gL / gR of the left/right
+// net updates (h, hu, hv, world frame), add the cotangents of the inputs to
+// outL / outR. QL / QR are the states (h = surface), dL / dR their depths,
+// sqL0 / sqR0 their sqrt(g * depth) as in the forward step.
+__device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL, const State& QR, double dL0,
+                                       double dR0, double sqL0, double sqR0, double drytol, const double gL[3],
+                                       const double gR[3], Grad4& outL, Grad4& outR) {
+    const double g = kG;
+    const double c = 0.5 * g;
+    // ---------------- forward (geoclaw_flux<FWAVE>, same expressions)
+    const double pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
+    const double pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
+    const double pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
+    const double pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+    double hL = dL0, hR = dR0, bL = QL.b, bR = QR.b;
+    if (hL <= drytol && hR <= drytol) return;  // no flux, no derivative
+    const bool wetR = hR > drytol, wetL = hL > drytol;
+    double huL, huR, uL, uR, vL, vR;
+    if (wetR) {
+        huR = pR1; uR = pR1 / hR; vR = pR2 / hR;
+    } else {
+        hR = 0.0; huR = 0.0; uR = 0.0; vR = 0.0;
+    }
+    if (wetL) {
+        huL = pL1; uL = pL1 / hL; vL = pL2 / hL;
+    } else {
+        hL = 0.0; huL = 0.0; uL = 0.0; vL = 0.0;
+    }
+    bool wall_l = false, wall_r = false, lower_l = false, lower_r = false;
+    if (!wetR) {
+        double hstar, s1m, s2m;
+        riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);
+        if (dmx(hL, hstar) + bL < bR) {
+            wall_r = true;
+            hR = hL; huR = -huL; bR = bL; uR = -uL; vR = vL;
+        } else if (hL + bL < bR) {
+            lower_r = true;
+            bR = hL + bL;
+        }
+    } else if (!wetL) {
+        double hstar, s1m, s2m;
+        riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);
+        if (dmx(hR, hstar) + bR < bL) {
+            wall_l = true;
+            hL = hR; huL = -huR; bL = bR; uL = -uR; vL = vR;
+        } else if (hR + bR < bL) {
+            lower_l = true;
+            bL = hR + bR;
+        }
+    }
+    const double X = ((bR + hR) - bL) - hL;
+    const double Hs = hR + hL;
+    const double dB = bR - bL;
+    const double sqL = (wetL || wall_l) ? (wall_l ? sqR0 : sqL0) : 0.0;
+    const double sqR = (wetR || wall_r) ? (wall_r ? sqL0 : sqR0) : 0.0;
+    const double sL = uL - sqL, sR = uR + sqR;
+    const double A = sqL * uL + sqR * uR, B = sqR + sqL;
+    const double uhat = A / B;
+    const double chat = sqrt((g * 0.5) * Hs);
+    const double r1 = uhat - chat, r2 = uhat + chat;
+    const bool e1_is_sL = sL < r1, e2_is_sR = sR > r2;
+    const double sE1 = e1_is_sL ? sL : r1, sE2 = e2_is_sR ? sR : r2;
+    const double delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) + ((c * X) * Hs)) - ((c * Hs) * dB);
+    const double delhu = huR - huL;
+    const double K = (g * 0.5) * Hs;
+    const double ddp = -(K * dB);
+    const double dpd = delphi - ddp;
+    const double D = sE2 - sE1;
+    const double beta1 = (sE2 * delhu - dpd) / D;
+    const double beta2 = (dpd - sE1 * delhu) / D;
+    const double sw[3] = {sE1, 0.5 * (sE1 + sE2), sE2};
+    // ---------------- reverse
+    // back-rotation p = net(2:3) T
+    double nL[3] = {gL[0], gL[1] * n1 + gL[2] * n2, -gL[1] * n2 + gL[2] * n1};
+    double nR[3] = {gR[0], gR[1] * n1 + gR[2] * n2, -gR[1] * n2 + gR[2] * n1};
+    // net-update split by wave-speed sign; walls remove waves
+    double F[3][3];
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {
+        const bool zeroed = (wall_l && w < 2) || (wall_r && w > 0);
+        const bool neg = sw[w] < 0.0, pos = sw[w] > 0.0;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            double f = neg ? nL[e] : (pos ? nR[e] : 0.5 * (nL[e] + nR[e]));
+            F[e][w] = zeroed ? 0.0 : f;
+        }
+    }
+    // fw(3,2) = ((huR vR - huL vL) - fw(3,1)) - fw(3,3); wave 2 carries no h / hu
+    double b_huR = F[2][1] * vR, b_vR = F[2][1] * huR, b_huL = -F[2][1] * vL, b_vL = -F[2][1] * huL;
+    const double F30 = F[2][0] - F[2][1], F32 = F[2][2] - F[2][1];
+    double b_beta1 = F[0][0] + F[1][0] * sE1 + F30 * vL;
+    double b_beta2 = F[0][2] + F[1][2] * sE2 + F32 * vR;
+    double b_sE1 = F[1][0] * beta1, b_sE2 = F[1][2] * beta2;
+    b_vL += F30 * beta1;
+    b_vR += F32 * beta2;
+    // beta1 = (sE2 delhu - dpd) / D, beta2 = (dpd - sE1 delhu) / D, D = sE2 - sE1
+    const double N1b = b_beta1 / D, N2b = b_beta2 / D;
+    const double b_D = -(b_beta1 * beta1 + b_beta2 * beta2) / D;
+    b_sE2 += N1b * delhu + b_D;
+    b_sE1 += -N2b * delhu - b_D;
+    double b_delhu = N1b * sE2 - N2b * sE1;
+    const double b_dpd = N2b - N1b;
+    // dpd = delphi - ddp, ddp = -(K dB), K = c Hs
+    double b_delphi = b_dpd;
+    const double b_ddp = -b_dpd;
+    double b_K = -b_ddp * dB;
+    double b_dB = -b_ddp * K;
+    double b_Hs = b_K * c;
+    // delhu = huR - huL
+    b_huR += b_delhu;
+    b_huL -= b_delhu;
+    // Einfeldt speeds
+    double b_sL = e1_is_sL ? b_sE1 : 0.0, b_r1 = e1_is_sL ? 0.0 : b_sE1;
+    double b_sR = e2_is_sR ? b_sE2 : 0.0, b_r2 = e2_is_sR ? 0.0 : b_sE2;
+    const double b_uhat = b_r1 + b_r2;
+    const double b_chat = b_r2 - b_r1;
+    if (chat > 0.0) b_Hs += b_chat * (0.5 / chat) * (g * 0.5);
+    double b_uL = b_sL, b_uR = b_sR;
+    double b_sqL = -b_sL, b_sqR = b_sR;
+    const double b_A = b_uhat / B, b_B = -b_uhat * uhat / B;
+    b_sqL += b_A * uL + b_B;
+    b_sqR += b_A * uR + b_B;
+    b_uL += b_A * sqL;
+    b_uR += b_A * sqR;
+    // delphi = ((T1 - T2) + T3) - T4
+    {
+        const double d = b_delphi;
+        const double su = uL + uR, dhu = huR - huL, uu = uL * uR, dh = hR - hL;
+        b_huR += d * su;
+        b_huL -= d * su;
+        b_uL += d * dhu - d * uR * dh;
+        b_uR += d * dhu - d * uL * dh;
+        double b_hR = -d * uu, b_hL = d * uu;
+        const double b_X = d * c * Hs;
+        b_Hs += d * (c * X) - d * c * dB;
+        b_dB += -d * (c * Hs);
+        // X = ((bR + hR) - bL) - hL
+        double b_bR = b_X, b_bL = -b_X;
+        b_hR += b_X;
+        b_hL -= b_X;
+        // Hs = hR + hL, dB = bR - bL
+        b_hR += b_Hs;
+        b_hL += b_Hs;
+        b_bR += b_dB;
+        b_bL -= b_dB;
+        // sqrt(g h) of the fixed-up depths
+        if (sqL > 0.0) b_hL += b_sqL * (0.5 * g / sqL);
+        if (sqR > 0.0) b_hR += b_sqR * (0.5 * g / sqR);
+        // undo the wall / lowering fix-ups: map the cotangents back to the original sides
+        double b_hL0 = 0.0, b_hR0 = 0.0, b_bL0 = 0.0, b_bR0 = 0.0;
+        if (wall_r) {  // hR = hL, huR = -huL, bR = bL, uR = -uL, vR = vL
+            b_hL += b_hR; b_hR = 0.0;
+            b_huL -= b_huR; b_huR = 0.0;
+            b_bL += b_bR; b_bR = 0.0;
+            b_uL -= b_uR; b_uR = 0.0;
+            b_vL += b_vR; b_vR = 0.0;
+        } else if (lower_r) {  // bR = hL + bL
+            b_hL += b_bR;
+            b_bL += b_bR;
+            b_bR = 0.0;
+        }
+        if (wall_l) {
+            b_hR += b_hL; b_hL = 0.0;
+            b_huR -= b_huL; b_huL = 0.0;
+            b_bR += b_bL; b_bL = 0.0;
+            b_uR -= b_uL; b_uL = 0.0;
+            b_vR += b_vL; b_vL = 0.0;
+        } else if (lower_l) {
+            b_hR += b_bL;
+            b_bR += b_bL;
+            b_bL = 0.0;
+        }
+        b_bL0 = b_bL;
+        b_bR0 = b_bR;
+        // wet extraction: u = hu / h, v = hv / h on wet sides; dry sides are constants
+        double b_pL1 = 0.0, b_pL2 = 0.0, b_pR1 = 0.0, b_pR2 = 0.0;
+        if (wetR) {
+            b_pR1 += b_huR + b_uR / hR;
+            b_pR2 += b_vR / hR;
+            b_hR0 = b_hR - (b_uR * uR + b_vR * vR) / hR;
+        }
+        if (wetL) {
+            b_pL1 += b_huL + b_uL / hL;
+            b_pL2 += b_vL / hL;
+            b_hL0 = b_hL - (b_uL * uL + b_vL * vL) / hL;
+        }
+        // depths h - b, rotations p_edge = T p
+        outL.h += b_hL0;
+        outL.b += b_bL0 - b_hL0;
+        outR.h += b_hR0;
+        outR.b += b_bR0 - b_hR0;
+        outL.hu += b_pL1 * n1 - b_pL2 * n2;
+        outL.hv += b_pL1 * n2 + b_pL2 * n1;
+        outR.hu += b_pR1 * n1 - b_pR2 * n2;
+        outR.hv += b_pR1 * n2 + b_pR2 * n1;
+    }
+}
+
+// Cotangent of a boundary ghost state pulled back to the cell (the ghost of
+// bnd_skeleton_scalar_op is a linear function of the cell state).
+template <int BC>
+__device__ __forceinline__ void boundary_ghost_vjp(double n1, double n2, const Grad4& gg, Grad4& out) {
+    out.h += gg.h;
+    out.b += gg.b;
+    if (BC == BC_SLIP) {  // p - (p . n) n
+        const double d = gg.hu * n1 + gg.hv * n2;
+        out.hu += gg.hu - d * n1;
+        out.hv += gg.hv - d * n2;
+    } else if (BC == BC_NOSLIP) {
+        out.hu -= gg.hu;
+        out.hv -= gg.hv;
+    } else {
+        out.hu += gg.hu;
+        out.hv += gg.hv;
+    }
+}
+
+struct AdjointArgs {
+    const double* h;          // x_t (state before the step)
+    const double* hu;
+    const double* hv;
+    const double* b;
+    const int8_t* depth;
+    const uint8_t* branch;    // per cell: bit 0 wetting fix fired, bit 1 drying clamp fired (forward step t)
+    const double* lam_h;      // cotangent of x_{t+1}
+    const double* lam_hu;
+    const double* lam_hv;
+    double* out_h;            // cotangent of x_t
+    double* out_hu;
+    double* out_hv;
+    double* bbar;             // += cotangent of b
+    const int4* tasks;
+    const long long* seg_ptr;
+    const int4* seg_info;
+    InstParams P;
+    double dt;
+    int32_t n_seg, seg_cells, n_cells_total, parity;
+    unsigned int* error;
+};
+
+// mu = -dt / volume * lambda' where the drying clamp did not fire: the
+// cotangent of the (length-weighted) sum of a cell's edge updates
+__device__ __forceinline__ void cell_mu(const AdjointArgs& A, int c, double ndv, double& m0, double& m1, double& m2) {
+    if (A.branch[c] & 2u) {
+        m0 = m1 = m2 = 0.0;
+    } else {
+        m0 = ndv * A.lam_h[c];
+        m1 = ndv * A.lam_hu[c];
+        m2 = ndv * A.lam_hv[c];
+    }
+}
+
+__global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int T = A.seg_cells;
+    double* sh_h = reinterpret_cast<double*>(smem_raw);
+    double* sh_hu = sh_h + T;
+    double* sh_hv = sh_hu + T;
+    double* sh_b = sh_hv + T;
+    double* sh_d = sh_b + T;
+    double* sh_sq = sh_d + T;
+    double* sh_mu = sh_sq + T;         // [3][T]
+    double* slot = sh_mu + 3 * T;      // [4 quantities][3 local edges][T]
+    const InstParams& P = A.P;
+    const int tid = threadIdx.x;
+    const int odd = A.parity & 1;
+
+    for (int seg = blockIdx.x; seg < A.n_seg; seg += gridDim.x) {
+        const int4 si = __ldg(&A.seg_info[seg]);
+        const int c0 = si.x, cn = si.y;
+        for (int i = tid; i < cn; i += blockDim.x) {
+            const int cc = c0 + i;
+            const double h = A.h[cc], b = A.b[cc];
+            sh_h[i] = h;
+            sh_hu[i] = A.hu[cc];
+            sh_hv[i] = A.hv[cc];
+            sh_b[i] = b;
+            double d, sq;
+            depth_terms(State{h, 0.0, 0.0, b}, P.drytol, d, sq);
+            sh_d[i] = d;
+            sh_sq[i] = sq;
+            const int dd = A.depth[cc];
+            const double vol = (P.scaling * P.scaling) * c_vol[dd];
+            double m0, m1, m2;
+            cell_mu(A, cc, -A.dt / vol, m0, m1, m2);
+            sh_mu[i] = m0;
+            sh_mu[T + i] = m1;
+            sh_mu[2 * T + i] = m2;
+            for (int k = 0; k < 12; ++k) slot[k * T + i] = 0.0;
+        }
+        __syncthreads();
+
+        const long long t0 = A.seg_ptr[seg], t1 = A.seg_ptr[seg + 1];
+        for (long long t = t0 + tid; t < t1; t += blockDim.x) {
+            const int4 tk = __ldg(&A.tasks[t]);
+            const uint32_t meta = (uint32_t)tk.z;
+            const bool bnd = (meta >> 14) & 1u;
+            int L, R, iL, iR, pL;
+            if (bnd || !odd) {
+                L = tk.x; iL = meta & 3u; pL = (meta >> 4) & 31u;
+                R = tk.y; iR = (meta >> 2) & 3u;
+            } else {
+                L = tk.y; iL = (meta >> 2) & 3u; pL = (meta >> 9) & 31u;
+                R = tk.x; iR = meta & 3u;
+            }
+            if ((unsigned)L >= (unsigned)A.n_cells_total || (!bnd && (unsigned)R >= (unsigned)A.n_cells_total) ||
+                iL > 2 || iR > 2 || pL > 16) {
+                atomicOr(A.error, 1u);
+                continue;
+            }
+            const double n1 = c_normal[pL][iL][0], n2 = c_normal[pL][iL][1];
+            const int sl = L - c0, sr = R - c0;
+            const bool lin = (unsigned)sl < (unsigned)cn;
+            const bool rin = !bnd && (unsigned)sr < (unsigned)cn;
+            State QL, QR;
+            double dL, dR, sqL, sqR, mL[3], mR[3] = {0.0, 0.0, 0.0};
+            int depL, depR = 0;
+            if (lin) {
+                QL = State{sh_h[sl], sh_hu[sl], sh_hv[sl], sh_b[sl]};
+                dL = sh_d[sl];
+                sqL = sh_sq[sl];
+                mL[0] = sh_mu[sl]; mL[1] = sh_mu[T + sl]; mL[2] = sh_mu[2 * T + sl];
+            } else {
+                QL = State{A.h[L], A.hu[L], A.hv[L], A.b[L]};
+                depth_terms(QL, P.drytol, dL, sqL);
+                const int dd = A.depth[L];
+                cell_mu(A, L, -A.dt / ((P.scaling * P.scaling) * c_vol[dd]), mL[0], mL[1], mL[2]);
+            }
+            depL = A.depth[L];
+            if (bnd) {
+                if (P.bc == BC_SLIP) QR = boundary_ghost<BC_SLIP>(n1, n2, QL);
+                else if (P.bc == BC_NOSLIP) QR = boundary_ghost<BC_NOSLIP>(n1, n2, QL);
+                else QR = QL;
+                dR = dL;
+                sqR = sqL;
+            } else {
+                if (rin) {
+                    QR = State{sh_h[sr], sh_hu[sr], sh_hv[sr], sh_b[sr]};
+                    dR = sh_d[sr];
+                    sqR = sh_sq[sr];
+                    mR[0] = sh_mu[sr]; mR[1] = sh_mu[T + sr]; mR[2] = sh_mu[2 * T + sr];
+                } else {
+                    QR = State{A.h[R], A.hu[R], A.hv[R], A.b[R]};
+                    depth_terms(QR, P.drytol, dR, sqR);
+                    const int dd = A.depth[R];
+                    cell_mu(A, R, -A.dt / ((P.scaling * P.scaling) * c_vol[dd]), mR[0], mR[1], mR[2]);
+                }
+                depR = A.depth[R];
+            }
+            // the edge's length in each cell: hypotenuse for local edge 2, else a leg
+            const double lenL = P.scaling * c_leg[iL == 1 ? depL : depL + 1];
+            const double gL[3] = {lenL * mL[0], lenL * mL[1], lenL * mL[2]};
+            double gR[3] = {0.0, 0.0, 0.0};
+            if (!bnd) {
+                const double lenR = P.scaling * c_leg[iR == 1 ? depR : depR + 1];
+                gR[0] = lenR * mR[0];
+                gR[1] = lenR * mR[1];
+                gR[2] = lenR * mR[2];
+            }
+            Grad4 oL{0.0, 0.0, 0.0, 0.0}, oR{0.0, 0.0, 0.0, 0.0};
+            fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, P.drytol, gL, gR, oL, oR);
+            if (bnd) {  // the ghost's cotangent goes back to the cell
+                if (P.bc == BC_SLIP) boundary_ghost_vjp<BC_SLIP>(n1, n2, oR, oL);
+                else if (P.bc == BC_NOSLIP) boundary_ghost_vjp<BC_NOSLIP>(n1, n2, oR, oL);
+                else boundary_ghost_vjp<BC_OUTFLOW>(n1, n2, oR, oL);
+            }
+            if (lin) {
+                slot[(0 * 3 + iL) * T + sl] = oL.h;
+                slot[(1 * 3 + iL) * T + sl] = oL.hu;
+                slot[(2 * 3 + iL) * T + sl] = oL.hv;
+                slot[(3 * 3 + iL) * T + sl] = oL.b;
+            }
+            if (rin) {
+                slot[(0 * 3 + iR) * T + sr] = oR.h;
+                slot[(1 * 3 + iR) * T + sr] = oR.hu;
+                slot[(2 * 3 + iR) * T + sr] = oR.hv;
+                slot[(3 * 3 + iR) * T + sr] = oR.b;
+            }
+        }
+        __syncthreads();
+
+        for (int i = tid; i < cn; i += blockDim.x) {
+            const int cc = c0 + i;
+            const uint8_t br = A.branch[cc];
+            const double lh = A.lam_h[cc], lu = A.lam_hu[cc], lv = A.lam_hv[cc];
+            double gh = 0.0, gu = 0.0, gv = 0.0, gb = 0.0;
+            if (br & 2u) {  // drying clamp: h' = min(b, 0), p' = 0
+                if (sh_b[i] < 0.0) gb += lh;
+            } else if (br & 1u) {  // wetting fix: h~ = b + drytol, p~ = 0
+                gb += lh;
+            } else {
+                gh = lh;
+                gu = lu;
+                gv = lv;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                gh += slot[(0 * 3 + k) * T + i];
+                gu += slot[(1 * 3 + k) * T + i];
+                gv += slot[(2 * 3 + k) * T + i];
+                gb += slot[(3 * 3 + k) * T + i];
+            }
+            A.out_h[cc] = gh;
+            A.out_hu[cc] = gu;
+            A.out_hv[cc] = gv;
+            A.bbar[cc] += gb;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace swe

@@ -48,6 +48,8 @@ struct InstScalars {
 struct GlobalScalars {
     unsigned int done;       // CTAs finished in the running step
     unsigned int error;      // nonzero: a kernel saw a bad index or a wait ran out
+    unsigned int next_seg;   // next segment to hand out in the running step
+    unsigned int pad;
     long long step;          // steps since the mesh upload (parity = traversal direction)
     long long dt_seq_base;   // step at which the frozen dt sequence starts
 };

@@ -26,13 +26,20 @@
 // summed in the other order.
 #pragma once
 
+// The kernels are compiled twice: in namespace swe with strict IEEE rounding
+// (no contraction) and in namespace swe_fma with FMA contraction (SWE_KNS).
+#ifndef SWE_KNS
+#define SWE_KNS swe
+#endif
+
 #include <cfloat>
 #include <cstdint>
 
 #include "swe_internal.h"
 #include "swe_riemann.cuh"
 
-namespace swe {
+namespace SWE_KNS {
+using namespace ::swe;
 
 __constant__ double c_leg[kMaxDepth + 2];  // sqrt(0.5)**i at [i + 1], i = -1..60
 __constant__ double c_vol[kMaxDepth + 1];  // 0.5**(i + 1)
@@ -51,6 +58,7 @@ struct StepArgs {
     const InstParams* ip;
     InstScalars* is;
     GlobalScalars* gs;
+    uint8_t* branch;           // optional per-cell output: bit 0 wetting fix, bit 1 drying clamp (adjoint)
     const double* dt_seq;      // frozen dt sequence [k * n_inst + inst] or null
     long long dt_seq_len;      // steps in the sequence
     int32_t n_seg, n_inst, seg_cells, max_ndepth, n_cells_total;
@@ -166,6 +174,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     __shared__ long long red_sum[32];
     __shared__ unsigned int s_error;
     __shared__ int s_last;
+    __shared__ int s_seg;
 
     const int tid = threadIdx.x;
     const long long step = A.gs->step;
@@ -191,7 +200,13 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     int cur = -1;
     InstParams P;
 
-    for (int seg = blockIdx.x; seg < A.n_seg; seg += gridDim.x) {
+    // segments are handed out dynamically (CTAs that draw cheap segments, e.g.
+    // dry land, take more); each CTA still sees its segments in increasing order
+    for (;;) {
+        if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+        __syncthreads();
+        const int seg = s_seg;
+        if (seg >= A.n_seg) break;
         const int4 si = __ldg(&A.seg_info[seg]);
         const int c0 = si.x, cn = si.y, inst = si.z;
         if (inst != cur) {  // uniform across the CTA
@@ -225,12 +240,14 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             sh_hv[i] = hvin[c0 + i];
             sh_b[i] = A.b[c0 + i];
         }
-        if (cbulk > 0) {
-            int polls = 0;
-            while (!mbar_try_wait(&bar, phase)) {
-                if (++polls > kWaitLimit) {
-                    s_error = 2u;
-                    break;
+        if (cbulk > 0) {  // one thread waits for the copy, the others at the barrier
+            if (tid == 0) {
+                int polls = 0;
+                while (!mbar_try_wait(&bar, phase)) {
+                    if (++polls > kWaitLimit) {
+                        s_error = 2u;
+                        break;
+                    }
                 }
             }
             phase ^= 1u;
@@ -338,10 +355,12 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             dp2 = ndv * dp2;
             double h = sh_h[i], p1 = sh_hu[i], p2 = sh_hv[i];
             const double b = sh_b[i];
+            uint8_t br = 0;
             if (h < b + P.drytol && dh > 0.0) {  // flooded land starts at the dry tolerance, at rest
                 h = b + P.drytol;
                 p1 = 0.0;
                 p2 = 0.0;
+                br = 1;
             }
             h = h + dh;
             p1 = p1 + dp1;
@@ -350,7 +369,9 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
                 h = dmn(b, 0.0);
                 p1 = 0.0;
                 p2 = 0.0;
+                br |= 2;
             }
+            if (A.branch) A.branch[c] = br;
             hout[c] = h;
             huout[c] = p1;
             hvout[c] = p2;
@@ -383,10 +404,11 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
         __syncthreads();
         if (tid == 0) {
             A.gs->done = 0;
+            A.gs->next_seg = 0;
             A.gs->step = step + 1;
             __threadfence();
         }
     }
 }
 
-}  // namespace swe
+}  // namespace SWE_KNS

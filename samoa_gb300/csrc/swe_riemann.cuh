@@ -9,9 +9,17 @@
 // instructions instead of spending an FP64 add.
 #pragma once
 
+// The kernels are compiled twice: in namespace swe with strict IEEE rounding
+// (no contraction) and in namespace swe_fma with FMA contraction (SWE_KNS).
+#ifndef SWE_KNS
+#define SWE_KNS swe
+#endif
+namespace swe {}
+
 #include <stdint.h>
 
-namespace swe {
+namespace SWE_KNS {
+using namespace ::swe;
 
 constexpr double kG = 9.80665;  // src/SWE/SWE_data_types.f90:34
 
@@ -415,4 +423,4 @@ __device__ __forceinline__ State boundary_ghost(double n1, double n2, const Stat
     return g;
 }
 
-}  // namespace swe
+}  // namespace SWE_KNS

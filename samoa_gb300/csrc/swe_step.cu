@@ -17,7 +17,7 @@
 #include <vector>
 
 #include "swe_internal.h"
-#include "swe_kernel.cuh"
+#include "swe_adjoint.cuh"
 
 namespace swe {
 
@@ -76,12 +76,24 @@ __global__ void reset_scalars_kernel(InstScalars* S, GlobalScalars* G, int n) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         G->done = 0;
         G->error = 0;
+        G->next_seg = 0;
         G->step = 0;
         G->dt_seq_base = 0;
     }
 }
 
 __global__ void mark_seq_base_kernel(GlobalScalars* G) { G->dt_seq_base = G->step; }
+
+__global__ void set_step_kernel(GlobalScalars* G, long long step) { G->step = step; }
+
+__global__ void gauge_kernel(const GlobalScalars* G, const double* h0, const double* h1, int64_t n,
+                             const int64_t* cells, int64_t n_cells, double* out) {
+    const double* h = (G->step & 1) ? h1 : h0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = cells[i];
+        out[i] = (c >= 0 && c < n_cells) ? h[c] : __longlong_as_double(0x7ff8000000000000LL);
+    }
+}
 
 typedef void (*StepKernel)(StepArgs);
 
@@ -97,6 +109,9 @@ static StepKernel kernel_for(int solver) {
     }
 }
 
+void* fma_step_kernel(int solver);
+cudaError_t fma_upload_tables();
+
 static int upload_tables() {
     // __constant__ symbols are per device: every context uploads for its device
     double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
@@ -104,6 +119,7 @@ static int upload_tables() {
     CUDA_TRY(cudaMemcpyToSymbol(c_leg, leg, sizeof(leg)));
     CUDA_TRY(cudaMemcpyToSymbol(c_vol, vol, sizeof(vol)));
     CUDA_TRY(cudaMemcpyToSymbol(c_normal, nrm, sizeof(nrm)));
+    CUDA_TRY(fma_upload_tables());
     return SWE_OK;
 }
 
@@ -124,7 +140,8 @@ struct swe_ctx {
     int64_t cells_packed = 0;      // sum of the instances' cells (host layout)
     bool has_mesh = false, has_state = false;
     // tiling
-    int32_t seg_cells = 512, block_threads = 256;
+    int32_t seg_cells = 512, block_threads = 128;  // the best of a sweep on GB300 (2^24 cells)
+    int32_t arith = SWE_ARITH_STRICT;
     int64_t n_seg = 0, n_tasks = 0;
     int grid = 0, max_ndepth = 1;
     size_t smem = 0;
@@ -143,6 +160,8 @@ struct swe_ctx {
     GlobalScalars* gs = nullptr;
     double* dt_seq = nullptr;
     int64_t dt_seq_len = 0;
+    std::vector<double> dt_seq_host;
+    uint8_t* branch = nullptr;      // wet/dry branch flags of the last forward step (adjoint)
     // CUDA graphs of n steps
     std::map<int64_t, cudaGraphExec_t> graphs;
     double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
@@ -164,7 +183,9 @@ void free_mesh_buffers(swe_ctx* c) {
         c->h[k] = c->hu[k] = c->hv[k] = nullptr;
     }
     cudaFree(c->b); cudaFree(c->depth); cudaFree(c->flags); cudaFree(c->tasks); cudaFree(c->seg_ptr);
-    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->dt_seq);
+    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->dt_seq); cudaFree(c->branch);
+    c->branch = nullptr;
+    c->dt_seq_host.clear();
     c->b = nullptr; c->depth = nullptr; c->flags = nullptr; c->tasks = nullptr; c->seg_ptr = nullptr;
     c->seg_info = nullptr; c->ip = nullptr; c->is = nullptr; c->dt_seq = nullptr; c->dt_seq_len = 0;
     c->has_mesh = c->has_state = false;
@@ -224,8 +245,10 @@ int configure_launch(swe_ctx* c) {
     c->smem = smem_bytes(c);
     StepKernel k = kernel_for(c->params.empty() ? FWAVE : c->params[0].solver);
     if (!k) return set_error(SWE_E_INVALID, "unknown solver");
-    for (int s : {FWAVE, AUG_RIEMANN, LF, LF_BATH, LLF, LLF_BATH})
+    for (int s : {FWAVE, AUG_RIEMANN, LF, LF_BATH, LLF, LLF_BATH}) {
         CUDA_TRY(cudaFuncSetAttribute(kernel_for(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+        CUDA_TRY(cudaFuncSetAttribute(fma_step_kernel(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    }
     int per_sm = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, c->block_threads, c->smem));
     if (per_sm < 1)
@@ -383,8 +406,9 @@ int copy_state(swe_ctx* c, int to_device, double* h, double* hu, double* hv, dou
     return SWE_OK;
 }
 
-int launch_steps(swe_ctx* c, int64_t n_steps) {
+int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr) {
     StepArgs A;
+    A.branch = branch;
     for (int k = 0; k < 2; ++k) {
         A.h[k] = c->h[k];
         A.hu[k] = c->hu[k];
@@ -407,11 +431,13 @@ int launch_steps(swe_ctx* c, int64_t n_steps) {
     A.max_ndepth = c->max_ndepth;
     A.n_cells_total = (int32_t)c->cells_total;
     A.use_tma = 1;
-    StepKernel k = kernel_for(c->params[0].solver);
-    for (int64_t s = 0; s < n_steps; ++s) {
-        k<<<c->grid, c->block_threads, c->smem, c->stream>>>(A);
-        CUDA_TRY(cudaGetLastError());
-    }
+    // the adjoint's forward step (branch output) always runs the strict kernel,
+    // so its branches are the ones the reverse sweep re-evaluates
+    void* k = (c->arith == SWE_ARITH_FMA && !branch) ? fma_step_kernel(c->params[0].solver)
+                                                     : (void*)kernel_for(c->params[0].solver);
+    void* args[] = {&A};
+    for (int64_t s = 0; s < n_steps; ++s)
+        CUDA_TRY(cudaLaunchKernel(k, dim3(c->grid), dim3(c->block_threads), args, c->smem, c->stream));
     return SWE_OK;
 }
 
@@ -542,6 +568,14 @@ int swe_set_tiling(swe_ctx* c, int32_t seg_cells, int32_t block_threads) {
     if (!c->has_mesh) return SWE_OK;
     cudaSetDevice(c->device);
     return rebuild_tasks(c);
+}
+
+int swe_set_arith(swe_ctx* c, int32_t mode) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (mode != SWE_ARITH_STRICT && mode != SWE_ARITH_FMA) return set_error(SWE_E_INVALID, "unknown arith mode %d", mode);
+    c->arith = mode;
+    drop_graphs(c);
+    return SWE_OK;
 }
 
 int swe_get_tiling(swe_ctx* c, int32_t* seg_cells, int32_t* block_threads) {
@@ -704,10 +738,145 @@ int swe_set_dt_sequence(swe_ctx* c, int64_t n_steps, const double* dts) {
     int rc = device_alloc((void**)&c->dt_seq, bytes);
     if (rc) return rc;
     CUDA_TRY(cudaMemcpyAsync(c->dt_seq, dts, bytes, cudaMemcpyHostToDevice, c->stream));
+    c->dt_seq_host.assign(dts, dts + (size_t)n_steps * (size_t)n_inst(c));
     mark_seq_base_kernel<<<1, 1, 0, c->stream>>>(c->gs);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->dt_seq_len = n_steps;
+    return SWE_OK;
+}
+
+int swe_snapshot_store(swe_ctx* c, double* h, double* hu, double* hv, int64_t* step) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "snapshots are for single-instance contexts");
+    if (!h || !hu || !hv) return set_error(SWE_E_INVALID, "null snapshot buffer");
+    cudaSetDevice(c->device);
+    long long s = 0;
+    CUDA_TRY(cudaMemcpyAsync(&s, &c->gs->step, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const int k = (int)(s & 1);
+    const size_t bytes = (size_t)c->mesh[0].n_cells * 8;
+    CUDA_TRY(cudaMemcpyAsync(h, c->h[k], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(hu, c->hu[k], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(hv, c->hv[k], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    if (step) *step = s;
+    return SWE_OK;
+}
+
+int swe_snapshot_restore(swe_ctx* c, const double* h, const double* hu, const double* hv, int64_t step) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (!c->has_mesh) return set_error(SWE_E_NOMESH, "upload a mesh first");
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "snapshots are for single-instance contexts");
+    if (!h || !hu || !hv || step < 0) return set_error(SWE_E_INVALID, "bad snapshot");
+    cudaSetDevice(c->device);
+    const int k = (int)(step & 1);
+    const size_t bytes = (size_t)c->mesh[0].n_cells * 8;
+    CUDA_TRY(cudaMemcpyAsync(c->h[k], h, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->hu[k], hu, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->hv[k], hv, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    set_step_kernel<<<1, 1, 0, c->stream>>>(c->gs, (long long)step);
+    CUDA_TRY(cudaGetLastError());
+    c->has_state = true;
+    return SWE_OK;
+}
+
+int swe_sample_gauges(swe_ctx* c, int64_t n_gauges, const int64_t* cells, double* out) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "gauges are for single-instance contexts");
+    if (n_gauges < 0 || (n_gauges > 0 && (!cells || !out))) return set_error(SWE_E_INVALID, "bad gauge arrays");
+    if (n_gauges == 0) return SWE_OK;
+    cudaSetDevice(c->device);
+    const int blocks = (int)std::min<int64_t>((n_gauges + 127) / 128, 1024);
+    gauge_kernel<<<blocks, 128, 0, c->stream>>>(c->gs, c->h[0], c->h[1], n_gauges, cells, c->mesh[0].n_cells, out);
+    CUDA_TRY(cudaGetLastError());
+    return SWE_OK;
+}
+
+int swe_traverse_branches(swe_ctx* c, int64_t n_steps, uint8_t* branch, int64_t stride) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_steps < 0 || (n_steps > 0 && !branch) || stride < c->cells_total)
+        return set_error(SWE_E_INVALID, "bad branch buffer (stride must be >= %lld)", (long long)c->cells_total);
+    cudaSetDevice(c->device);
+    for (int64_t s = 0; s < n_steps; ++s)
+        if ((rc = launch_steps(c, 1, branch + s * stride))) return rc;
+    return SWE_OK;
+}
+
+int swe_step_back(swe_ctx* c) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (!c->has_mesh) return set_error(SWE_E_NOMESH, "upload a mesh first");
+    cudaSetDevice(c->device);
+    long long s = 0;
+    CUDA_TRY(cudaMemcpyAsync(&s, &c->gs->step, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (s < 1) return set_error(SWE_E_STATE, "no step to go back from");
+    set_step_kernel<<<1, 1, 0, c->stream>>>(c->gs, s - 1);
+    CUDA_TRY(cudaGetLastError());
+    return SWE_OK;
+}
+
+int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, const double* lam_hu,
+                     const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
+    if (c->params[0].solver != SWE_SOLVER_FWAVE)
+        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave solver");
+    if (!lam_h || !lam_hu || !lam_hv || !out_h || !out_hu || !out_hv || !bbar)
+        return set_error(SWE_E_INVALID, "null cotangent buffer");
+    cudaSetDevice(c->device);
+    GlobalScalars g;
+    CUDA_TRY(cudaMemcpyAsync(&g, c->gs, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const long long t = g.step, k = t - g.dt_seq_base;
+    if (!c->dt_seq || k < 0 || k >= c->dt_seq_len)
+        return set_error(SWE_E_STATE, "the adjoint needs a frozen dt sequence covering step %lld", t);
+    if (!branch) {
+        // forward step t -> t+1 recording the branches; x_t stays in buffer t & 1
+        if (!c->branch && (rc = device_alloc((void**)&c->branch, (size_t)c->cells_total))) return rc;
+        if ((rc = launch_steps(c, 1, c->branch))) return rc;
+        branch = c->branch;
+    }
+    AdjointArgs A;
+    const int in = (int)(t & 1);
+    A.h = c->h[in];
+    A.hu = c->hu[in];
+    A.hv = c->hv[in];
+    A.b = c->b;
+    A.depth = c->depth;
+    A.branch = branch;
+    A.lam_h = lam_h;
+    A.lam_hu = lam_hu;
+    A.lam_hv = lam_hv;
+    A.out_h = out_h;
+    A.out_hu = out_hu;
+    A.out_hv = out_hv;
+    A.bbar = bbar;
+    A.tasks = reinterpret_cast<const int4*>(c->tasks);
+    A.seg_ptr = c->seg_ptr;
+    A.seg_info = reinterpret_cast<const int4*>(c->seg_info);
+    CUDA_TRY(cudaMemcpyAsync(&A.P, c->ip, sizeof(InstParams), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    A.dt = c->dt_seq_host[(size_t)k];
+    A.n_seg = (int32_t)c->n_seg;
+    A.seg_cells = c->seg_cells;
+    A.n_cells_total = (int32_t)c->cells_total;
+    A.parity = (int32_t)(t & 1);
+    A.error = &c->gs->error;
+    // the reverse kernel holds more registers per thread than the step: it runs
+    // 256 threads per CTA so an SM still has two CTAs' worth of warps
+    const int threads = 256;
+    const size_t smem = (size_t)21 * c->seg_cells * sizeof(double);
+    CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, threads, smem));
+    if (per_sm < 1) return set_error(SWE_E_INVALID, "adjoint tiling does not fit an SM");
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * c->num_sms, c->n_seg));
+    adjoint_kernel<<<grid, threads, smem, c->stream>>>(A);
+    CUDA_TRY(cudaGetLastError());
     return SWE_OK;
 }
 

