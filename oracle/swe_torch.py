@@ -44,6 +44,39 @@ def _sqrt(x):
     return _ExactSqrt.apply(x)
 
 
+class BranchTape:
+    """Records the outcome of every branch of the flux in evaluation order and
+    replays it: with a replayed tape the step is the branch-frozen function
+    whose derivative the adjoint computes, so finite differences of it do not
+    straddle the kinks of min/max and sign switches."""
+
+    def __init__(self):
+        self.items = []
+        self.pos = 0
+        self.replay = False
+
+    def start(self, replay):
+        self.replay = replay
+        self.pos = 0
+        if not replay:
+            self.items = []
+
+    def cmp(self, value):
+        if self.replay:
+            v = self.items[self.pos]
+            self.pos += 1
+            return v
+        self.items.append(value)
+        return value
+
+
+_NOTAPE = None
+
+
+def _cmp(tape, value):
+    return value if tape is None else tape.cmp(value)
+
+
 def _where(c, a, b):
     return torch.where(c, a, b)
 
@@ -87,7 +120,7 @@ def _riemann_structure_hstar(hL, hR, uL, uR, drytol):
     return torch.where(h_min <= drytol, torch.zeros_like(hm), hm)
 
 
-def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol):
+def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
     """compute_geoclaw_flux with the f-wave solver, vectorised over edges.
     Returns the left and right net updates (h, hu, hv) in world coordinates."""
     g = G
@@ -99,9 +132,9 @@ def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol):
     pR2 = -n2 * pxR + n1 * pyR
     hL = hsL - bL
     hR = hsR - bR
-    active = ~((hL <= drytol) & (hR <= drytol))
-    wetR = hR > drytol
-    wetL = hL > drytol
+    active = _cmp(tape, ~((hL <= drytol) & (hR <= drytol)))
+    wetR = _cmp(tape, hR > drytol)
+    wetL = _cmp(tape, hL > drytol)
     hRs = _where(wetR, hR, one)
     hLs = _where(wetL, hL, one)
     uR = _where(wetR, pR1 / hRs, zero)
@@ -118,11 +151,11 @@ def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol):
     rdry = ~wetR
     ldry = (~rdry) & (~wetL)
     hst_r = _riemann_structure_hstar(hL, hL, uL, -uL, drytol)
-    wall_r = rdry & (_dmx(hL.detach(), hst_r) + bL < bR)
-    lower_r = rdry & (~wall_r) & (hL + bL < bR)
+    wall_r = _cmp(tape, rdry & (_dmx(hL.detach(), hst_r) + bL < bR))
+    lower_r = _cmp(tape, rdry & (~wall_r) & (hL + bL < bR))
     hst_l = _riemann_structure_hstar(hR, hR, -uR, uR, drytol)
-    wall_l = ldry & (_dmx(hR.detach(), hst_l) + bR < bL)
-    lower_l = ldry & (~wall_l) & (hR + bR < bL)
+    wall_l = _cmp(tape, ldry & (_dmx(hR.detach(), hst_l) + bR < bL))
+    lower_l = _cmp(tape, ldry & (~wall_l) & (hR + bR < bL))
     hR_, huR_, bR_, uR_, vR_ = (_where(wall_r, hL, hR), _where(wall_r, -huL, huR), _where(wall_r, bL, bR),
                                 _where(wall_r, -uL, uR), _where(wall_r, vL, vR))
     bR_ = _where(lower_r, hL + bL, bR_)
@@ -144,8 +177,9 @@ def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol):
     uhat = (sqL * uL + sqR * uR) / _where(den > 0, den, one)
     ch_in = (g * 0.5) * (hR + hL)
     chat = _sqrt(_where(ch_in > 0, ch_in, one)) * (ch_in > 0)
-    sE1 = _dmn(sL, uhat - chat)
-    sE2 = _dmx(sR, uhat + chat)
+    r1, r2 = uhat - chat, uhat + chat
+    sE1 = _where(_cmp(tape, sL < r1), sL, r1)
+    sE2 = _where(_cmp(tape, sR > r2), sR, r2)
     delhu = huR - huL
     delb = bR - bL
     deldelphi = -(((g * 0.5) * (hR + hL)) * delb)
@@ -164,9 +198,10 @@ def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol):
             fw[e][w] = _where(walls[w], fw[e][w] * 0.0, fw[e][w])
     netL = [zero, zero, zero]
     netR = [zero, zero, zero]
+    signs = [(_cmp(tape, sw[w] < 0.0), _cmp(tape, sw[w] > 0.0)) for w in range(3)]
     for e in range(3):
         for w in range(3):
-            neg, pos = sw[w] < 0.0, sw[w] > 0.0
+            neg, pos = signs[w]
             f = fw[e][w]
             netL[e] = _where(neg, netL[e] + f, _where(pos, netL[e], netL[e] + 0.5 * f))
             netR[e] = _where(pos, netR[e] + f, _where(neg, netR[e], netR[e] + 0.5 * f))
@@ -212,14 +247,15 @@ class TorchStep:
         self.hyp = scaling * leg[d]
         self.vol = (scaling * scaling) * vol[d]
 
-    def step(self, h, hu, hv, b, dt, parity):
+    def step(self, h, hu, hv, b, dt, parity, tape=None):
         n = self.n
         odd = parity & 1
         if odd:
             L, R, iL, iR, nn = self.eb, self.ea, self.lb, self.la, self.nB
         else:
             L, R, iL, iR, nn = self.ea, self.eb, self.la, self.lb, self.nA
-        fL, fR = fwave_flux(nn[:, 0], nn[:, 1], h[L], hu[L], hv[L], b[L], h[R], hu[R], hv[R], b[R], self.drytol)
+        fL, fR = fwave_flux(nn[:, 0], nn[:, 1], h[L], hu[L], hv[L], b[L], h[R], hu[R], hv[R], b[R], self.drytol,
+                            tape)
         c = self.bcell
         n1, n2 = self.nBnd[:, 0], self.nBnd[:, 1]
         gp1, gp2 = hu[c], hv[c]
@@ -228,7 +264,7 @@ class TorchStep:
             gp1, gp2 = hu[c] - dd * n1, hv[c] - dd * n2
         elif self.bc == "noslip":
             gp1, gp2 = -hu[c], -hv[c]
-        fB, _ = fwave_flux(n1, n2, h[c], hu[c], hv[c], b[c], h[c], gp1, gp2, b[c], self.drytol)
+        fB, _ = fwave_flux(n1, n2, h[c], hu[c], hv[c], b[c], h[c], gp1, gp2, b[c], self.drytol, tape)
         # slot values [cell, local edge]
         slots = []
         for q in range(3):
@@ -244,18 +280,31 @@ class TorchStep:
             s = slots[q]
             d.append((self.leg * s[:, k0] + self.hyp * s[:, 1]) + self.leg * s[:, k2])
         dh, dp1, dp2 = (sc * x for x in d)
-        wet_fix = (h < b + self.drytol) & (dh > 0.0)
+        wet_fix = _cmp(tape, (h < b + self.drytol) & (dh > 0.0))
         h1 = _where(wet_fix, b + self.drytol, h)
         p1 = _where(wet_fix, torch.zeros_like(hu), hu)
         p2 = _where(wet_fix, torch.zeros_like(hv), hv)
         h1 = h1 + dh
         p1 = p1 + dp1
         p2 = p2 + dp2
-        dry = h1 < b + self.drytol
+        dry = _cmp(tape, h1 < b + self.drytol)
         h1 = _where(dry, _dmn(b, torch.zeros_like(b)), h1)
         p1 = _where(dry, torch.zeros_like(p1), p1)
         p2 = _where(dry, torch.zeros_like(p2), p2)
         return h1, p1, p2
+
+
+def gauge_objective_frozen(tstep, h0, hu0, hv0, b, dts, gauges, obs, tapes, replay):
+    """J with every step's branches recorded into (replay=False) or replayed
+    from (replay=True) the per-step tapes."""
+    x = (h0, hu0, hv0)
+    J = 0.0
+    with torch.no_grad():
+        for t, dt in enumerate(dts):
+            tapes[t].start(replay)
+            x = tstep.step(*x, b, float(dt), t, tapes[t])
+            J += float(((x[0][gauges] - obs[t]) ** 2).sum())
+    return J
 
 
 def gauge_objective_and_grad(tstep, h0, hu0, hv0, b, dts, gauges, obs, parity0=0, need_grad=True):

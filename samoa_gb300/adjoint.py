@@ -218,11 +218,12 @@ class GaugeProblem:
         return J, gh, bbar
 
 
-def time_steps(problem, k=50):
+def time_steps(problem, h0, b, k=50):
     """Seconds per forward step and per reverse step (the adjoint kernel with
-    recorded branches), on the problem's mesh, from its initial state."""
+    recorded branches), on the problem's mesh, from the state (h0, b)."""
     P = problem
     L = P.ctx.L
+    P._set_initial(h0, b)
     with torch.cuda.stream(P.stream):
         lam = torch.zeros((3, P.n), dtype=torch.float64, device=P.dev)
         out = torch.zeros_like(lam)
