@@ -241,6 +241,14 @@ int swe_mesh_validate(int64_t n_cells, const int8_t* depth, const int8_t* plotte
 int swe_riemann_batch(int32_t solver, int64_t n, const double* normals, const double* q_left, const double* q_right,
                       double dry_tolerance, double* out_left, double* out_right);
 
+/* Device self-check of the step's correctly rounded division with a shared
+ * reciprocal (the quotients u = hu / h and v = hv / h, which share h, and the
+ * two f-wave coefficients, which share s2 - s1): on 2n seeded random pairs
+ * (a, b) with exponents in [-exponent_span, exponent_span], one in 16 with
+ * a = 0, counts the quotients that differ from IEEE a / b in any bit.
+ * No counterpart in the reference (the Fortran step divides directly). */
+int swe_division_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t* mismatches);
+
 /* One time step on caller-owned device memory, allocating nothing. No
  * counterpart in the reference. For callers that cannot allocate device memory
  * at the point where they step (a host code whose device memory all comes from

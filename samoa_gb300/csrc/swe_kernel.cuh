@@ -162,8 +162,8 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     double* sh_hu = sh_h + T;
     double* sh_hv = sh_hu + T;
     double* sh_b = sh_hv + T;
-    double* sh_d = sh_b + T;        // depth h - b
-    double* sh_sq = sh_d + T;       // sqrt(g * depth) where the cell is wet
+    double* sh_rh = sh_b + T;       // RN(1 / depth) where the cell is wet
+    double* sh_sq = sh_rh + T;      // sqrt(g * depth) where the cell is wet
     double* upd = sh_sq + T;        // [4 quantities][3 local edges][T cells]
     double* tab_leg = upd + 12 * T; // per depth of the current instance
     double* tab_hyp = tab_leg + A.max_ndepth;
@@ -255,9 +255,9 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
         __syncthreads();
         if (s_error) break;
         for (int i = tid; i < cn; i += blockDim.x) {
-            double d, sq;
-            depth_terms(State{sh_h[i], 0.0, 0.0, sh_b[i]}, P.drytol, d, sq);
-            sh_d[i] = d;
+            double d, sq, y;
+            depth_terms(State{sh_h[i], 0.0, 0.0, sh_b[i]}, P.drytol, d, sq, y);
+            sh_rh[i] = y;
             sh_sq[i] = sq;
         }
         __syncthreads();
@@ -286,14 +286,15 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             const bool lin = (unsigned)sl < (unsigned)cn;
             const bool rin = !bnd && (unsigned)sr < (unsigned)cn;
             State QL, QR;
-            double dL, dR, sqL, sqR;
+            double dL, dR, sqL, sqR, yL, yR;
             if (lin) {
                 QL = State{sh_h[sl], sh_hu[sl], sh_hv[sl], sh_b[sl]};
-                dL = sh_d[sl];
+                dL = QL.h - QL.b;
                 sqL = sh_sq[sl];
+                yL = sh_rh[sl];
             } else {
                 QL = State{hin[L], huin[L], hvin[L], A.b[L]};
-                depth_terms(QL, P.drytol, dL, sqL);
+                depth_terms(QL, P.drytol, dL, sqL, yL);
             }
             if (bnd) {  // the ghost has the cell's h and b
                 if (P.bc == BC_SLIP) QR = boundary_ghost<BC_SLIP>(n1, n2, QL);
@@ -301,16 +302,18 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
                 else QR = QL;
                 dR = dL;
                 sqR = sqL;
+                yR = yL;
             } else if (rin) {
                 QR = State{sh_h[sr], sh_hu[sr], sh_hv[sr], sh_b[sr]};
-                dR = sh_d[sr];
+                dR = QR.h - QR.b;
                 sqR = sh_sq[sr];
+                yR = sh_rh[sr];
             } else {
                 QR = State{hin[R], huin[R], hvin[R], A.b[R]};
-                depth_terms(QR, P.drytol, dR, sqR);
+                depth_terms(QR, P.drytol, dR, sqR, yR);
             }
             Update fL, fR;
-            edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, P.drytol, fL, fR);
+            edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, fL, fR);
             if (lin) {
                 upd[(0 * 3 + iL) * T + sl] = fL.h;
                 upd[(1 * 3 + iL) * T + sl] = fL.p1;

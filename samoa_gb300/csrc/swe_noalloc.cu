@@ -117,11 +117,11 @@ __global__ void edges_kernel(Args A, unsigned char* scratch) {
         } else {
             QR = load(A, R);
         }
-        double dL, dR, sqL, sqR;
-        depth_terms(QL, A.drytol, dL, sqL);
-        depth_terms(QR, A.drytol, dR, sqR);
+        double dL, dR, sqL, sqR, yL, yR;
+        depth_terms(QL, A.drytol, dL, sqL, yL);
+        depth_terms(QR, A.drytol, dR, sqR, yR);
         Update fL, fR;
-        edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, A.drytol, fL, fR);
+        edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, A.drytol, fL, fR);
         slots[(0 * 3 + iL) * M + L] = fL.h;
         slots[(1 * 3 + iL) * M + L] = fL.p1;
         slots[(2 * 3 + iL) * M + L] = fL.p2;

@@ -40,6 +40,71 @@ __device__ __forceinline__ double z0(double x) {
 __device__ __forceinline__ double dmn(double a, double b) { return (a < b) ? a : b; }
 __device__ __forceinline__ double dmx(double a, double b) { return (a > b) ? a : b; }
 
+// ---------------------------------------------------------------------------
+// Correctly rounded division with a shared reciprocal.
+// Several quotients in the step share a divisor (a cell's depth divides its
+// edges' normal and tangential momenta; the two f-wave coefficients share
+// s2 - s1). recip_rn computes y = RN(1/b) once: two Newton-Raphson steps from
+// the hardware approximation bring y within one ulp of 1/b, and a third step
+// with an exact residual e = 1 - b y rounds it correctly unless b's significand
+// is all ones (Markstein's reciprocal theorem). div_rn then gets RN(a/b) from y:
+// q0 = RN(a y) is within 1.5 ulp of a/b, one correction q1 = RN(q0 + (a - b q0) y)
+// brings it well inside one ulp, and a second correction is Markstein's
+// division theorem: if y = RN(1/b) and q is within one ulp of a/b, then
+// r = a - b q is exact and RN(q + r y) = RN(a/b) (P. Markstein, IBM J. Res.
+// Dev. 34(1), 1990; M. Cornea-Hasegan, R. Golliver, P. Markstein, ARITH-14,
+// 1999). The exponents of a and b are kept within [-500, 500], where no
+// intermediate result under- or overflows; outside that range, for a zero
+// divisor and for the all-ones significand, plain IEEE division is used. All
+// tests are integer operations, so the FP64 pipe only sees the arithmetic.
+// swe_division_check compares the results with IEEE division on the device.
+__device__ __forceinline__ double rcp_approx(double b) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(b));
+    return y;
+}
+
+struct Recip {
+    double b, y;
+    bool fast;
+};
+
+__device__ __forceinline__ bool exp_in(double x, int lo, int hi) {
+    const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+    return e >= lo && e <= hi;
+}
+
+__device__ __forceinline__ bool recip_fast(double b) {
+    const long long bits = __double_as_longlong(b);
+    return exp_in(b, -500, 500) && ((bits & 0x000fffffffffffffLL) != 0x000fffffffffffffLL);
+}
+
+__device__ __forceinline__ Recip recip_rn(double b) {
+    Recip r;
+    r.b = b;
+    r.fast = recip_fast(b);
+    double y = rcp_approx(b);
+    double e = fma(-b, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-b, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-b, y, 1.0);
+    r.y = fma(y, e, y);
+    return r;
+}
+
+__device__ __forceinline__ double div_rn(double a, const Recip& r) {
+    if (!r.fast) return a / r.b;
+    if ((__double_as_longlong(a) << 1) == 0) return a * r.y;  // +-0 with the IEEE sign
+    if (!exp_in(a, -500, 500)) return a / r.b;
+    double q = a * r.y;
+    double res = fma(-r.b, q, a);
+    q = fma(res, r.y, q);
+    res = fma(-r.b, q, a);
+    return fma(res, r.y, q);
+}
+
+
 // Riemann structure with one Newton step, src/geoclaw/riemannsolvers.f:507-618.
 static __device__ __noinline__ void riemann_structure(double hL, double hR, double uL, double uR, double drytol,
                                                double& hm, double& s1m, double& s2m) {
@@ -178,10 +243,12 @@ static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL
 // sqL0 / sqR0 are sqrt(g * depth) of the two cells, computed once per cell by the
 // caller; they are used only where the reference evaluates sqrt(g * h) on an
 // unmodified wet depth (the same operands, so the same bits).
+// yL0 / yR0 are RN(1 / depth) of the two cells (read only for wet sides).
 template <int SOLVER>
 __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL, double huR, double hvL,
                                                double hvR, double bL, double bR, double sqL0, double sqR0,
-                                               double drytol, double netL[3], double netR[3], double& maxspeed) {
+                                               double yL0, double yR0, double drytol, double netL[3],
+                                               double netR[3], double& maxspeed) {
     const double g = kG;
     netL[0] = netL[1] = netL[2] = 0.0;
     netR[0] = netR[1] = netR[2] = 0.0;
@@ -189,14 +256,16 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     if (hL <= drytol && hR <= drytol) return;
     double uL, uR, vL, vR;
     if (hR > drytol) {
-        uR = huR / hR;
-        vR = hvR / hR;
+        const Recip r{hR, yR0, recip_fast(hR)};
+        uR = div_rn(huR, r);
+        vR = div_rn(hvR, r);
     } else {
         hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0;
     }
     if (hL > drytol) {
-        uL = huL / hL;
-        vL = hvL / hL;
+        const Recip r{hL, yL0, recip_fast(hL)};
+        uL = div_rn(huL, r);
+        vL = div_rn(hvL, r);
     } else {
         hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0;
     }
@@ -245,8 +314,9 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         double delb = bR - bL;
         double deldelphi = -(((g * 0.5) * (hR + hL)) * delb);
         double dpd = delphi - deldelphi;
-        double beta1 = (sE2 * delhu - dpd) / (sE2 - sE1);
-        double beta2 = (dpd - sE1 * delhu) / (sE2 - sE1);
+        const Recip rD = recip_rn(sE2 - sE1);
+        double beta1 = div_rn(sE2 * delhu - dpd, rD);
+        double beta2 = div_rn(dpd - sE1 * delhu, rD);
         sw[0] = sE1; sw[1] = 0.5 * (sE1 + sE2); sw[2] = sE2;
         fw[0][0] = beta1; fw[1][0] = beta1 * sE1; fw[2][0] = beta1 * vL;
         fw[0][2] = beta2; fw[1][2] = beta2 * sE2; fw[2][2] = beta2 * vR;
@@ -302,15 +372,15 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
 // compute_geoclaw_flux, src/SWE/SWE_euler_timestep.f90:449-481
 template <int SOLVER>
 __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR, double dL,
-                                             double dR, double sqL, double sqR, double drytol, Update& fL,
-                                             Update& fR) {
+                                             double dR, double sqL, double sqR, double yL, double yR,
+                                             double drytol, Update& fL, Update& fR) {
     // T = [[n1, n2], [-n2, n1]]; p_edge = T p
     double pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
     double pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
     double pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
     double pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
     double netL[3], netR[3], ms;
-    geoclaw_solver<SOLVER>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, drytol, netL, netR, ms);
+    geoclaw_solver<SOLVER>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, yL, yR, drytol, netL, netR, ms);
     // p = net(2:3) T
     fL.h = netL[0];
     fL.p1 = z0(netL[1] * n1) + netL[2] * -n2;
@@ -392,20 +462,29 @@ __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, c
 }
 
 // One edge: dL/dR are the depths h - b of the two states, sqL/sqR their
-// sqrt(g * depth) (only read for depths above the dry tolerance).
+// sqrt(g * depth) and yL/yR RN(1 / depth) (only read for depths above the dry
+// tolerance).
 template <int SOLVER>
 __device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL, const State& QR, double dL,
-                                          double dR, double sqL, double sqR, double drytol, Update& fL, Update& fR) {
+                                          double dR, double sqL, double sqR, double yL, double yR, double drytol,
+                                          Update& fL, Update& fR) {
     if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
-        geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, drytol, fL, fR);
+        geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR);
     else
         lf_flux<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, fL, fR);
 }
 
-// depth and sqrt(g * depth) of a state, as the edge code needs them
+// depth, sqrt(g * depth) and RN(1 / depth) of a state, as the edge code needs them
 __device__ __forceinline__ void depth_terms(const State& Q, double drytol, double& d, double& sq) {
     d = Q.h - Q.b;
     sq = d > drytol ? sqrt(kG * d) : 0.0;
+}
+
+__device__ __forceinline__ void depth_terms(const State& Q, double drytol, double& d, double& sq, double& y) {
+    d = Q.h - Q.b;
+    const bool wet = d > drytol;
+    sq = wet ? sqrt(kG * d) : 0.0;
+    y = wet ? recip_rn(d).y : 0.0;
 }
 
 // Ghost state of bnd_skeleton_scalar_op, src/SWE/SWE_euler_timestep.f90:231-255.

@@ -45,14 +45,57 @@ __global__ void riemann_batch_kernel(int64_t n, const double* nrm, const double*
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         State L{ql[4 * i], ql[4 * i + 1], ql[4 * i + 2], ql[4 * i + 3]};
         State R{qr[4 * i], qr[4 * i + 1], qr[4 * i + 2], qr[4 * i + 3]};
-        double dL, dR, sqL, sqR;
-        depth_terms(L, drytol, dL, sqL);
-        depth_terms(R, drytol, dR, sqR);
+        double dL, dR, sqL, sqR, yL, yR;
+        depth_terms(L, drytol, dL, sqL, yL);
+        depth_terms(R, drytol, dR, sqR, yR);
         Update fL, fR;
-        edge_flux<SOLVER>(nrm[2 * i], nrm[2 * i + 1], L, R, dL, dR, sqL, sqR, drytol, fL, fR);
+        edge_flux<SOLVER>(nrm[2 * i], nrm[2 * i + 1], L, R, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR);
         ol[4 * i] = fL.h; ol[4 * i + 1] = fL.p1; ol[4 * i + 2] = fL.p2; ol[4 * i + 3] = fL.s;
         orr[4 * i] = fR.h; orr[4 * i + 1] = fR.p1; orr[4 * i + 2] = fR.p2; orr[4 * i + 3] = fR.s;
     }
+}
+
+// splitmix64 (Steele, Lea, Flood, OOPSLA 2014): a counter-based stream of
+// 64-bit values for the division self-check.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// A double with a random significand, random sign and an exponent drawn from
+// [-e_span, e_span]; every 8th value gets an all-ones or all-zeros low
+// significand, which exercises the tie and boundary cases of the rounding.
+__device__ __forceinline__ double draw_double(unsigned long long z, int e_span) {
+    const unsigned long long w = mix64(z);
+    unsigned long long mant = w & 0x000fffffffffffffULL;
+    const int sel = (int)((w >> 52) & 7);
+    if (sel == 0) mant |= 0x000ffffffff00000ULL;
+    if (sel == 1) mant &= 0x000ffffff0000000ULL;
+    const unsigned long long r = mix64(z ^ 0x5555555555555555ULL);
+    const int e = (int)(r % (unsigned long long)(2 * e_span + 1)) - e_span;
+    const unsigned long long sign = (r >> 63) << 63;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | mant));
+}
+
+// Compares div_rn(a, recip_rn(b)) and div_rn(c, recip_rn(b)) with the IEEE
+// quotients bit for bit (a NaN matches any NaN); counts mismatches.
+__global__ void division_check_kernel(int64_t n, unsigned long long seed, int e_span,
+                                      unsigned long long* mismatches) {
+    unsigned long long bad = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long z = seed + 3ULL * (unsigned long long)i;
+        const double b = draw_double(z, e_span);
+        const double a = draw_double(z + 1, e_span);
+        const double c = (i & 15) == 0 ? 0.0 : draw_double(z + 2, e_span);
+        const Recip r = recip_rn(b);
+        const double q1 = div_rn(a, r), q2 = div_rn(c, r), e1 = a / b, e2 = c / b;
+        const bool ok1 = (q1 != q1 && e1 != e1) || __double_as_longlong(q1) == __double_as_longlong(e1);
+        const bool ok2 = (q2 != q2 && e2 != e2) || __double_as_longlong(q2) == __double_as_longlong(e2);
+        bad += (ok1 ? 0 : 1) + (ok2 ? 0 : 1);
+    }
+    if (bad) atomicAdd(mismatches, bad);
 }
 
 __global__ void set_times_kernel(InstScalars* S, const double* t, const double* dt, int n) {
@@ -966,6 +1009,27 @@ int swe_riemann_batch(int32_t solver, int64_t n, const double* normals, const do
     if (e == cudaSuccess) e = cudaMemcpy(out_right, orr, 32 * (size_t)n, cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return set_error(SWE_E_CUDA, "riemann batch: %s", cudaGetErrorString(e));
+    return SWE_OK;
+}
+
+int swe_division_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t* mismatches) {
+    if (n < 0 || !mismatches || exponent_span < 0 || exponent_span > 1022)
+        return set_error(SWE_E_INVALID, "bad arguments");
+    *mismatches = 0;
+    if (n == 0) return SWE_OK;
+    unsigned long long* d = nullptr;
+    int rc = device_alloc((void**)&d, sizeof(unsigned long long));
+    if (rc) return rc;
+    cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        division_check_kernel<<<1216, 256>>>(n, (unsigned long long)seed, exponent_span, d);
+        e = cudaGetLastError();
+    }
+    unsigned long long got = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&got, d, sizeof(got), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return set_error(SWE_E_CUDA, "division check: %s", cudaGetErrorString(e));
+    *mismatches = (int64_t)got;
     return SWE_OK;
 }
 

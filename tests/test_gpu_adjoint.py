@@ -108,7 +108,9 @@ def test_gauge_gradient_matches_cpu_adjoint(swe_lib):
 def test_gradient_matches_central_differences_h0(swe_lib):
     """Deep basin, 200 steps, 6 seeded random directions of the initial
     displacement: central differences of J on the GPU (frozen dt sequence)
-    agree with the adjoint gradient within 1e-6 relative."""
+    agree with the adjoint gradient within 1e-6 relative. The step is 1e-5 of
+    max|h0|: J carries ~1e-14 relative round-off, and at 1e-6 that is already
+    1e-6 of the smaller directional derivatives (1e-2 of J)."""
     case = scenarios.adjoint_case(log2_cells=12, steps=200, n_gauges=16, seed=5)
     P = adjoint.GaugeProblem(case["mesh"], case["params"], case["gauges"], case["obs"], case["dts"], snapshots=8)
     try:
@@ -117,7 +119,7 @@ def test_gradient_matches_central_differences_h0(swe_lib):
         rng = np.random.default_rng(16)
         for k in range(6):
             d = rng.normal(size=case["h0"].shape)
-            eps = 1e-6 * np.abs(case["h0"]).max()
+            eps = 1e-5 * np.abs(case["h0"]).max()
             Jp = P.objective(case["h0"] + eps * d, case["b"], record=False)
             Jm = P.objective(case["h0"] - eps * d, case["b"], record=False)
             fd, ad = (Jp - Jm) / (2 * eps), float(gh @ d)
@@ -131,7 +133,10 @@ def test_bathymetry_gradient_matches_branch_frozen_differences(swe_lib):
     objective: J has kinks (the Einfeldt min/max and the middle wave's sign
     switch wherever neighbouring depths or velocities cross), so plain
     differences straddle them; replaying every branch of the unperturbed run
-    (torch FP64 restatement) gives the function the adjoint differentiates."""
+    (torch FP64 restatement) gives the function the adjoint differentiates.
+    The step is 1e-4 of max|b|: the directional derivatives here are ~1e-6 of
+    J, so smaller steps are limited by J's round-off; the frozen function is
+    smooth, and the truncation error at this step is below 1e-7."""
     import torch
     case = scenarios.adjoint_case(log2_cells=10, steps=60, n_gauges=8, seed=7)
     P = adjoint.GaugeProblem(case["mesh"], case["params"], case["gauges"], case["obs"], case["dts"], snapshots=6)
@@ -149,7 +154,7 @@ def test_bathymetry_gradient_matches_branch_frozen_differences(swe_lib):
     J0 = ST.gauge_objective_frozen(T, h0, z, z, b, case["dts"], g, obs, tapes, False)
     assert abs(J0 - J) <= 1e-12 * abs(J)
     rng = np.random.default_rng(17)
-    eps = 1e-6 * float(np.abs(case["b"]).max())
+    eps = 1e-4 * float(np.abs(case["b"]).max())
     for k in range(4):
         d = rng.normal(size=mesh.n_cells)
         dt_ = torch.tensor(d)

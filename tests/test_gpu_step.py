@@ -256,3 +256,15 @@ def test_fma_mode_within_tolerance(swe_lib, oracle_lib, solver):
             assert np.array_equal(flags, S.flags)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("span", [30, 500, 1022])
+def test_division_with_shared_reciprocal_is_ieee(swe_lib, span):
+    """The step's quotients by a shared reciprocal (Markstein's correction) equal
+    IEEE division bit for bit: 2 x 2^24 seeded pairs per exponent span, the
+    widest one reaching the ranges where plain division takes over."""
+    import ctypes as C
+    from samoa_gb300 import _lib
+    bad = C.c_int64(-1)
+    _lib.check(swe_lib.swe_division_check(1 << 24, 1234 + span, span, C.byref(bad)))
+    assert bad.value == 0
