@@ -299,34 +299,40 @@ def adjoint_compare(a, device):
         stats = dict(P.stats)
         gh, gb = gh.cpu().numpy(), gb.cpu().numpy()
         rng = np.random.default_rng(16)
-        worst = {"h0": 0.0, "b": 0.0}
-        for k in range(a.adjoint_fd):
-            d = rng.normal(size=gh.shape)
-            if k % 2 == 0:
-                eps = 1e-6 * float(np.abs(case["h0"]).max())
-                Jp = P.objective(case["h0"] + eps * d, case["b"], record=False)
-                Jm = P.objective(case["h0"] - eps * d, case["b"], record=False)
-                ad = float(gh @ d)
-            else:
-                eps = 1e-6 * float(np.abs(case["b"]).max())
-                Jp = P.objective(case["h0"], case["b"] + eps * d, record=False)
-                Jm = P.objective(case["h0"], case["b"] - eps * d, record=False)
-                ad = float(gb @ d)
-            key = "h0" if k % 2 == 0 else "b"
-            worst[key] = max(worst[key], abs((Jp - Jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
+        # directions supported off the flat -20 m shelf: there neighbouring depths
+        # are equal, every edge sits on the Einfeldt min/max kink, and central
+        # differences straddle it
+        deep = case["b"] < -100.0
+        errs = {"h0": [], "b": []}
+        for key, n_dir in (("h0", a.adjoint_fd), ("b", max(1, a.adjoint_fd // 4))):
+            for k in range(n_dir):
+                d = rng.normal(size=gh.shape) * deep
+                if key == "h0":
+                    eps = 1e-6 * float(np.abs(case["h0"]).max())
+                    Jp = P.objective(case["h0"] + eps * d, case["b"], record=False)
+                    Jm = P.objective(case["h0"] - eps * d, case["b"], record=False)
+                    ad = float(gh @ d)
+                else:
+                    eps = 1e-6 * float(np.abs(case["b"]).max())
+                    Jp = P.objective(case["h0"], case["b"] + eps * d, record=False)
+                    Jm = P.objective(case["h0"], case["b"] - eps * d, record=False)
+                    ad = float(gb @ d)
+                errs[key].append(abs((Jp - Jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
         t_step, t_adj = adjoint.time_steps(P, case["h0"], case["b"], 50)
     finally:
         P.close()
     n = case["mesh"].n_cells
     return {"cells": n, "steps": a.adjoint_steps, "snapshots": 64, "J": J, "forward_s": t_fwd, "gradient_s": t_grad,
             "gradient_over_forward": t_grad / t_fwd, "forward_steps_in_gradient": stats["forward_steps"],
-            "adjoint_steps": stats["adjoint_steps"], "fd_directions": a.adjoint_fd,
-            "fd_max_rel_err_h0": worst["h0"], "fd_max_rel_err_b_unfrozen": worst["b"],
+            "adjoint_steps": stats["adjoint_steps"], "fd_directions_h0": len(errs["h0"]),
+            "fd_max_rel_err_h0": max(errs["h0"]), "fd_median_rel_err_h0": float(np.median(errs["h0"])),
+            "fd_directions_b": len(errs["b"]), "fd_max_rel_err_b_unfrozen": max(errs["b"]),
             "forward_step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj, "adjoint_step_over_forward_step": t_adj / t_step,
             "note": "gradient_s = one checkpointed sweep (its first descent is the forward run; recomputation "
-                    "included); J(h0, b) is the squared misfit at 32 gauges; dt frozen, FD with the same dts; the "
-                    "b directions cross the Einfeldt min/max kinks, so plain FD there is limited by them (the "
-                    "branch-frozen FD check of b is in the tests)"}
+                    "included); J(h0, b) is the squared misfit at 32 gauges; dt frozen, FD with the same dts, "
+                    "eps = 1e-6 relative, seeded N(0,1) directions on the cells deeper than 100 m; perturbing b "
+                    "reorders neighbouring depths at rest and so crosses the Einfeldt min/max kinks over 2,000 "
+                    "steps, so plain FD in b is kink-limited (the branch-frozen FD check of b is in the tests)"}
 
 
 def run_gpu(a, rank, world, local):

@@ -14,23 +14,29 @@ constexpr int kMaxDepth = 60;  // bit_size(int64) - 4, src/SFC_data_types.f90:77
 // One edge task of a segment: 16 bytes, loaded with one 128-bit load.
 //   a, b: cells (b = -1 for a domain-boundary edge); on an inner edge a < b.
 //   meta: bits 0-1 local edge index of a (0..2), bits 2-3 of b,
-//         bits 4-8 plotter type of a + 8, bits 9-13 of b + 8, bit 14 boundary.
+//         bits 4-8 plotter type of a + 8, bits 9-13 of b + 8, bit 14 boundary,
+//         bits 15-16 normal direction: 0 diagonal, 1 along x, 2 along y (the
+//         same for both cells: their normals are opposite).
 struct alignas(16) Task {
     int32_t a, b;
     uint32_t meta;
     uint32_t pad;
 };
 
-inline uint32_t pack_meta(int la, int lb, int pa, int pb, bool bnd) {
+inline uint32_t pack_meta(int la, int lb, int pa, int pb, bool bnd, int axis = 0) {
     return (uint32_t)la | ((uint32_t)lb << 2) | ((uint32_t)(pa + 8) << 4) | ((uint32_t)(pb + 8) << 9) |
-           ((uint32_t)(bnd ? 1 : 0) << 14);
+           ((uint32_t)(bnd ? 1 : 0) << 14) | ((uint32_t)axis << 15);
 }
 
 // Per-instance parameters on the device (the cfg fields the step reads,
 // src/Config.f90:30-121, plus the depth range present in the instance's mesh).
+// dt_by_max: the cell volumes are exactly RN(scaling^2) * 2^-(d+1) for every
+// depth of the mesh (no underflow), so min over cells of RN(volume / ds) equals
+// RN(RN(scaling^2) / max over cells of ds * 2^(d+1)) and the step divides once
+// per instance instead of once per cell.
 struct InstParams {
     double drytol, courant, scaling, thr_refine, thr_coarsen, max_time, tout;
-    int32_t min_depth, max_depth, dmin, ndepth, bc, pad;
+    int32_t min_depth, max_depth, dmin, ndepth, bc, dt_by_max;
 };
 
 // Per-instance scalars on the device. The step kernel reads dt, reduces into
@@ -41,6 +47,7 @@ struct InstScalars {
     double dt;                      // grid%r_dt for the next step
     double dt_new;                  // min(volume / sum(len * speed)) of the last step
     unsigned long long dt_acc;      // bits of the running minimum (non-negative doubles order as integers)
+    unsigned long long ds_acc;      // bits of the running maximum of ds * 2^(d+1) (dt_by_max)
     unsigned long long refine_acc;  // refinements issued in the running step
     unsigned long long n_refine;    // refinements issued in the last step
 };

@@ -110,6 +110,15 @@ __device__ __forceinline__ double warp_min(double v) {
     return v;
 }
 
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
 __device__ __forceinline__ long long warp_sum(long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -126,31 +135,38 @@ __device__ __forceinline__ double step_dt(const StepArgs& A, const InstParams& P
     return dt;
 }
 
-// Block-wide reduction of (dtmin, nref) into instance `inst`; all threads call it.
-__device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, double& dtmin, long long& nref,
-                                               double* red_min, long long* red_sum) {
+// Block-wide reduction of (dtmin, dskey, nref) into instance `inst`; all threads call it.
+__device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, double& dtmin, unsigned long long& dskey,
+                                               long long& nref, double* red_min, unsigned long long* red_max,
+                                               long long* red_sum) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     double m = warp_min(dtmin);
+    unsigned long long x = warp_max_u64(dskey);
     long long s = warp_sum(nref);
     if (lane == 0) {
         red_min[warp] = m;
+        red_max[warp] = x;
         red_sum[warp] = s;
     }
     __syncthreads();
     if (warp == 0) {
         const int nw = (blockDim.x + 31) >> 5;
         m = lane < nw ? red_min[lane] : DBL_MAX;
+        x = lane < nw ? red_max[lane] : 0ull;
         s = lane < nw ? red_sum[lane] : 0;
         m = warp_min(m);
+        x = warp_max_u64(x);
         s = warp_sum(s);
         if (lane == 0) {
             // non-negative doubles order like their bit patterns
-            atomicMin(&A.is[inst].dt_acc, (unsigned long long)__double_as_longlong(m));
+            if (m != DBL_MAX) atomicMin(&A.is[inst].dt_acc, (unsigned long long)__double_as_longlong(m));
+            if (x) atomicMax(&A.is[inst].ds_acc, x);
             if (s) atomicAdd(&A.is[inst].refine_acc, (unsigned long long)s);
         }
     }
     __syncthreads();
     dtmin = DBL_MAX;
+    dskey = 0;
     nref = 0;
 }
 
@@ -169,8 +185,10 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     double* tab_hyp = tab_leg + A.max_ndepth;
     double* tab_vol = tab_hyp + A.max_ndepth;
     double* tab_ndv = tab_vol + A.max_ndepth;  // -dt / volume
+    double* tab_pow = tab_ndv + A.max_ndepth;  // 2^(d+1)
     __shared__ uint64_t bar;
     __shared__ double red_min[32];
+    __shared__ unsigned long long red_max[32];
     __shared__ long long red_sum[32];
     __shared__ unsigned int s_error;
     __shared__ int s_last;
@@ -195,6 +213,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     __syncthreads();
 
     double dtmin = DBL_MAX;  // r_dt_new = huge(1.0) (pre_traversal_op, :133-140)
+    unsigned long long dskey = 0;  // bits of max ds * 2^(d+1) (dt_by_max)
     long long nref = 0;
     uint32_t phase = 0;
     int cur = -1;
@@ -210,7 +229,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
         const int4 si = __ldg(&A.seg_info[seg]);
         const int c0 = si.x, cn = si.y, inst = si.z;
         if (inst != cur) {  // uniform across the CTA
-            if (cur >= 0) flush_instance(A, cur, dtmin, nref, red_min, red_sum);
+            if (cur >= 0) flush_instance(A, cur, dtmin, dskey, nref, red_min, red_max, red_sum);
             P = A.ip[inst];
             const double dt = step_dt(A, P, inst, kseq);
             for (int i = tid; i < P.ndepth; i += blockDim.x) {
@@ -220,6 +239,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
                 tab_hyp[i] = P.scaling * c_leg[d];
                 tab_vol[i] = vol;
                 tab_ndv[i] = -dt / vol;
+                tab_pow[i] = ldexp(2.0, d);
             }
             cur = inst;
         }
@@ -313,7 +333,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
                 depth_terms(QR, P.drytol, dR, sqR, yR);
             }
             Update fL, fR;
-            edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, fL, fR);
+            edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, fL, fR, (int)((meta >> 15) & 3u));
             if (lin) {
                 upd[(0 * 3 + iL) * T + sl] = fL.h;
                 upd[(1 * 3 + iL) * T + sl] = fL.p1;
@@ -335,7 +355,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             const int c = c0 + i;
             const int d = A.depth[c];
             const int di = d - P.dmin;
-            const double leg = tab_leg[di], hyp = tab_hyp[di], vol = tab_vol[di], ndv = tab_ndv[di];
+            const double leg = tab_leg[di], hyp = tab_hyp[di], ndv = tab_ndv[di];
             double dh = z0(leg * upd[(0 * 3 + k0) * T + i]) + hyp * upd[(0 * 3 + 1) * T + i];
             dh = dh + leg * upd[(0 * 3 + k2) * T + i];
             double dp1 = z0(leg * upd[(1 * 3 + k0) * T + i]) + hyp * upd[(1 * 3 + 1) * T + i];
@@ -352,7 +372,12 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             } else if (d > P.min_depth && nrm < P.thr_coarsen) {
                 f = -1;
             }
-            dtmin = dmn(dtmin, vol / ds);
+            if (P.dt_by_max) {  // ds >= 0, so its bits order like its value
+                const unsigned long long x = (unsigned long long)__double_as_longlong(ds * tab_pow[di]);
+                dskey = x > dskey ? x : dskey;
+            } else {
+                dtmin = dmn(dtmin, tab_vol[di] / ds);
+            }
             dh = ndv * dh;
             dp1 = ndv * dp1;
             dp2 = ndv * dp2;
@@ -384,7 +409,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     }
 
     // ---- 4. reductions and the last-CTA finalisation (post_traversal_grid_op, :111-131)
-    if (cur >= 0) flush_instance(A, cur, dtmin, nref, red_min, red_sum);
+    if (cur >= 0) flush_instance(A, cur, dtmin, dskey, nref, red_min, red_max, red_sum);
     if (tid == 0) {
         if (s_error) atomicOr(&A.gs->error, s_error);
         __threadfence();
@@ -397,12 +422,15 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             const InstParams Q = A.ip[i];
             const double dt = step_dt(A, Q, i, kseq);
             InstScalars* S = &A.is[i];
-            const double dtn = __longlong_as_double((long long)atomicAdd(&S->dt_acc, 0ull));
+            double dtn = __longlong_as_double((long long)atomicAdd(&S->dt_acc, 0ull));
+            const unsigned long long x = atomicAdd(&S->ds_acc, 0ull);
+            if (x) dtn = dmn(dtn, (Q.scaling * Q.scaling) / __longlong_as_double((long long)x));
             S->time = S->time + dt;
             S->dt_new = dtn;
             S->dt = Q.courant * dtn;
             S->n_refine = atomicExch(&S->refine_acc, 0ull);
             S->dt_acc = (unsigned long long)__double_as_longlong(DBL_MAX);
+            S->ds_acc = 0;
         }
         __syncthreads();
         if (tid == 0) {

@@ -175,6 +175,22 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
 // a task in both (each keeps its own side, so no segment waits for another). A
 // boundary edge is a task in its cell's segment. Boundary tasks come first in a
 // segment, then inner edges in stream (first-touch) order.
+// Direction of the outward normal of local edge k (0..2) of a cell with plotter
+// type p: 1 = along x, 2 = along y, 0 = diagonal.
+static int normal_axis(int p, int k) {
+    static double normal[17][3][2];
+    static bool ready = false;
+    if (!ready) {
+        double leg[kMaxDepth + 2], vol[kMaxDepth + 1];
+        geometry_tables(leg, vol, normal);
+        ready = true;
+    }
+    const double* n = normal[p + 8][k];
+    if (n[1] == 0.0 && n[0] != 0.0) return 1;
+    if (n[0] == 0.0 && n[1] != 0.0) return 2;
+    return 0;
+}
+
 int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std::vector<int64_t>& seg_ptr,
                 std::vector<SegInfo>& seg_info, std::vector<Task>& tasks) {
     const int64_t n = m.n_cells;
@@ -208,7 +224,8 @@ int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std:
         Task t;
         t.a = (int32_t)(offset + c);
         t.b = -1;
-        t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true);
+        t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true,
+                           normal_axis(m.plotter[(size_t)c], m.bl[(size_t)j] - 1));
         t.pad = 0;
         tasks[(size_t)fill[(size_t)(c / T)]++] = t;
     }
@@ -217,11 +234,18 @@ int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std:
         Task t;
         t.a = (int32_t)(offset + a);
         t.b = (int32_t)(offset + b);
-        t.meta = pack_meta(m.la[(size_t)e] - 1, m.lb[(size_t)e] - 1, m.plotter[(size_t)a], m.plotter[(size_t)b], false);
+        t.meta = pack_meta(m.la[(size_t)e] - 1, m.lb[(size_t)e] - 1, m.plotter[(size_t)a], m.plotter[(size_t)b], false,
+                           normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1));
         t.pad = 0;
         int64_t sa = a / T, sb = b / T;
         tasks[(size_t)fill[(size_t)sa]++] = t;
         if (sb != sa) tasks[(size_t)fill[(size_t)sb]++] = t;
+    }
+    // within a segment, diagonal edges first, then the axis-aligned ones, so a
+    // warp's tasks mostly take the same branch of the flux's rotation
+    for (int64_t s = 0; s < nseg; ++s) {
+        auto first = tasks.begin() + (base + count[(size_t)s]), last = tasks.begin() + (base + count[(size_t)s + 1]);
+        std::stable_partition(first, last, [](const Task& t) { return ((t.meta >> 15) & 3u) == 0; });
     }
     return SWE_OK;
 }

@@ -40,6 +40,25 @@ __device__ __forceinline__ double z0(double x) {
 __device__ __forceinline__ double dmn(double a, double b) { return (a < b) ? a : b; }
 __device__ __forceinline__ double dmx(double a, double b) { return (a > b) ? a : b; }
 
+// IEEE predicates on the integer pipe (bit patterns), exact for every input
+// including +-0, infinities and NaN; the FP64 pipe is the step's bottleneck.
+__device__ __forceinline__ long long abs_bits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+__device__ __forceinline__ bool not_nan(long long a) { return a <= 0x7ff0000000000000LL; }  // a = abs_bits
+__device__ __forceinline__ bool is_finite(double x) { return abs_bits(x) < 0x7ff0000000000000LL; }
+__device__ __forceinline__ bool lt0(double x) {  // x < 0.0
+    const long long b = __double_as_longlong(x);
+    const long long a = b & 0x7fffffffffffffffLL;
+    return b < 0 && a != 0 && not_nan(a);
+}
+__device__ __forceinline__ bool gt0(double x) {  // x > 0.0
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+}
+// x with its sign flipped when `neg` (exact, like multiplying by -1)
+__device__ __forceinline__ double flip(double x, bool neg) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+}
+
 // ---------------------------------------------------------------------------
 // Correctly rounded division with a shared reciprocal.
 // Several quotients in the step share a divisor (a cell's depth divides its
@@ -68,6 +87,17 @@ struct Recip {
     double b, y;
     bool fast;
 };
+
+// 1/b to about one ulp (two Newton-Raphson steps from the hardware
+// approximation), for cotangents, which need no correct rounding; b must be
+// a normal number.
+__device__ __forceinline__ double rcp_nr(double b) {
+    double y = rcp_approx(b);
+    double e = fma(-b, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-b, y, 1.0);
+    return fma(y, e, y);
+}
 
 __device__ __forceinline__ bool exp_in(double x, int lo, int hi) {
     const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
@@ -301,7 +331,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     double sqR = wetR ? (wall_r ? sqL0 : sqR0) : 0.0;
     double sL = uL - sqL;
     double sR = uR + sqR;
-    double uhat = (sqL * uL + sqR * uR) / (sqR + sqL);
+    double uhat = div_rn(sqL * uL + sqR * uR, recip_rn(sqR + sqL));
     double chat = sqrt((g * 0.5) * (hR + hL));
     double sE1 = dmn(sL, uhat - chat);
     double sE2 = dmx(sR, uhat + chat);
@@ -347,7 +377,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     };
 #pragma unroll
     for (int w = 0; w < 3; ++w) {
-        const bool neg = sw[w] < 0.0, pos = sw[w] > 0.0;
+        const bool neg = lt0(sw[w]), pos = gt0(sw[w]);
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
             if (SOLVER != AUG_RIEMANN && w == 1 && e < 2) continue;
@@ -363,33 +393,64 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
             }
         }
     }
-    double m = fabs(sw[0]);
-    if (fabs(sw[1]) > m) m = fabs(sw[1]);
-    if (fabs(sw[2]) > m) m = fabs(sw[2]);
-    maxspeed = m;
+    // m = |s1|; if (|s2| > m) m = |s2|; if (|s3| > m) m = |s3|, on the bit
+    // patterns (non-negative values order like them; a NaN candidate never wins)
+    long long m = abs_bits(sw[0]);
+    const long long a1 = abs_bits(sw[1]), a2 = abs_bits(sw[2]);
+    if (a1 > m && not_nan(a1)) m = a1;
+    if (a2 > m && not_nan(a2)) m = a2;
+    maxspeed = __longlong_as_double(m);
 }
 
-// compute_geoclaw_flux, src/SWE/SWE_euler_timestep.f90:449-481
+// compute_geoclaw_flux, src/SWE/SWE_euler_timestep.f90:449-481.
+// axis: 0 = any normal; 1 = n = (+-1, +0); 2 = n = (+0, +-1). For an
+// axis-aligned normal each component of T p and of net(2:3) T is one exact
+// product plus a signed zero, i.e. the other momentum with its sign flipped
+// and -0 mapped to +0, which integer instructions give bit for bit while the
+// operands are finite (0 * inf would be NaN); otherwise the general form runs.
 template <int SOLVER>
 __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR, double dL,
                                              double dR, double sqL, double sqR, double yL, double yR,
-                                             double drytol, Update& fL, Update& fR) {
-    // T = [[n1, n2], [-n2, n1]]; p_edge = T p
-    double pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
-    double pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
-    double pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
-    double pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+                                             double drytol, Update& fL, Update& fR, int axis = 0) {
+    const bool fast = axis != 0 && is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
+    const bool sn = axis == 1 ? lt0(n1) : lt0(n2);  // sign of the nonzero component
+    double pL1, pL2, pR1, pR2;
+    if (fast) {
+        if (axis == 1) {
+            pL1 = z0(flip(QL.p1, sn)); pL2 = z0(flip(QL.p2, sn));
+            pR1 = z0(flip(QR.p1, sn)); pR2 = z0(flip(QR.p2, sn));
+        } else {
+            pL1 = z0(flip(QL.p2, sn)); pL2 = z0(flip(QL.p1, !sn));
+            pR1 = z0(flip(QR.p2, sn)); pR2 = z0(flip(QR.p1, !sn));
+        }
+    } else {
+        // T = [[n1, n2], [-n2, n1]]; p_edge = T p
+        pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
+        pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
+        pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
+        pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+    }
     double netL[3], netR[3], ms;
     geoclaw_solver<SOLVER>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, yL, yR, drytol, netL, netR, ms);
-    // p = net(2:3) T
     fL.h = netL[0];
-    fL.p1 = z0(netL[1] * n1) + netL[2] * -n2;
-    fL.p2 = z0(netL[1] * n2) + netL[2] * n1;
     fL.s = ms;
     fR.h = netR[0];
-    fR.p1 = z0(netR[1] * n1) + netR[2] * -n2;
-    fR.p2 = z0(netR[1] * n2) + netR[2] * n1;
     fR.s = ms;
+    if (fast && is_finite(netL[1]) && is_finite(netL[2]) && is_finite(netR[1]) && is_finite(netR[2])) {
+        if (axis == 1) {
+            fL.p1 = z0(flip(netL[1], sn)); fL.p2 = z0(flip(netL[2], sn));
+            fR.p1 = z0(flip(netR[1], sn)); fR.p2 = z0(flip(netR[2], sn));
+        } else {
+            fL.p1 = z0(flip(netL[2], !sn)); fL.p2 = z0(flip(netL[1], sn));
+            fR.p1 = z0(flip(netR[2], !sn)); fR.p2 = z0(flip(netR[1], sn));
+        }
+    } else {
+        // p = net(2:3) T
+        fL.p1 = z0(netL[1] * n1) + netL[2] * -n2;
+        fL.p2 = z0(netL[1] * n2) + netL[2] * n1;
+        fR.p1 = z0(netR[1] * n1) + netR[2] * -n2;
+        fR.p2 = z0(netR[1] * n2) + netR[2] * n1;
+    }
 }
 
 __device__ __forceinline__ double normal_velocity(double n1, double n2, double p1, double p2, double d) {
@@ -467,9 +528,9 @@ __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, c
 template <int SOLVER>
 __device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL, const State& QR, double dL,
                                           double dR, double sqL, double sqR, double yL, double yR, double drytol,
-                                          Update& fL, Update& fR) {
+                                          Update& fL, Update& fR, int axis = 0) {
     if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
-        geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR);
+        geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, axis);
     else
         lf_flux<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, fL, fR);
 }

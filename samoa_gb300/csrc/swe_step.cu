@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -103,6 +104,7 @@ __global__ void set_times_kernel(InstScalars* S, const double* t, const double* 
         S[i].time = t[i];
         S[i].dt = dt[i];
         S[i].dt_acc = (unsigned long long)__double_as_longlong(DBL_MAX);
+        S[i].ds_acc = 0;
         S[i].refine_acc = 0;
     }
 }
@@ -113,6 +115,7 @@ __global__ void reset_scalars_kernel(InstScalars* S, GlobalScalars* G, int n) {
         S[i].dt = 0.0;
         S[i].dt_new = DBL_MAX;
         S[i].dt_acc = (unsigned long long)__double_as_longlong(DBL_MAX);
+        S[i].ds_acc = 0;
         S[i].refine_acc = 0;
         S[i].n_refine = 0;
     }
@@ -245,7 +248,7 @@ int device_alloc(void** p, size_t bytes) {
 }
 
 size_t smem_bytes(const swe_ctx* c) {
-    return (size_t)18 * c->seg_cells * sizeof(double) + (size_t)4 * c->max_ndepth * sizeof(double);
+    return (size_t)18 * c->seg_cells * sizeof(double) + (size_t)5 * c->max_ndepth * sizeof(double);
 }
 
 int check_params(const swe_params* p) {
@@ -277,7 +280,10 @@ int upload_inst_params(swe_ctx* c) {
         q.dmin = c->mesh[(size_t)i].min_depth;
         q.ndepth = c->mesh[(size_t)i].max_depth - c->mesh[(size_t)i].min_depth + 1;
         q.bc = p.bc;
-        q.pad = 0;
+        // RN(scaling^2) * 2^-(d+1) must stay a normal number for the deepest cell
+        const double v0 = p.scaling * p.scaling;
+        const int dmax = c->mesh[(size_t)i].max_depth;
+        q.dt_by_max = (std::isfinite(v0) && v0 > 0.0 && std::ldexp(v0, -(dmax + 1)) >= DBL_MIN) ? 1 : 0;
     }
     CUDA_TRY(cudaMemcpyAsync(c->ip, v.data(), sizeof(InstParams) * v.size(), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
