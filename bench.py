@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--log2-cells", type=int, default=26)
     ap.add_argument("--solver", default="fwave")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-tune", action="store_true", help="skip the tiling autotuner (default tiling)")
+    ap.add_argument("--tune-log2-cells", type=int, default=22)
     ap.add_argument("--cpu-sample-log2", type=int, default=22)
     ap.add_argument("--cpu-steps", type=int, default=8)
     ap.add_argument("--segment-cells", type=int, default=0)
@@ -353,8 +355,18 @@ def run_gpu(a, rank, world, local):
     ctx = swe.SweContext(local)
     ctx.set_params(scn.cfg.params())
     ctx.set_arith(a.arith)
+    tuning = None
     if a.segment_cells or a.block_threads:
         ctx.set_tiling(a.segment_cells, a.block_threads)
+    elif not a.no_tune:  # the autotuner on a sample of the same basin (not timed)
+        from samoa_gb300 import autotune
+        sample = scenarios.ocean_basin(log2_cells=min(a.tune_log2_cells, a.log2_cells), solver=a.solver,
+                                       device="cuda")
+        sg = sample.grid
+        best, res = autotune.autotune(sg.mesh, sg.h, sg.hu, sg.hv, sg.b, sample.cfg.params(), sg.r_dt, device=local)
+        ctx.set_tiling(*best)
+        tuning = {"sample_cells": sg.mesh.n_cells, "best": list(best),
+                  "ms_per_step": {"%dx%d" % k: round(v * 1e3, 4) for k, v in sorted(res.items())}}
     ctx.upload_mesh(g.mesh)
     ctx.upload_state(g.h, g.hu, g.hv, g.b)
     ctx.set_time(g.r_time, g.r_dt)
@@ -390,32 +402,51 @@ def run_gpu(a, rank, world, local):
     sim_time, dt, _ = ctx.get_time()
     value = n * a.steps * world / (ms * 1e-3)
 
-    # end to end through the public API with host buffers: every step uploads
-    # the state from pinned host memory, runs the step, reads the state and the
-    # refinement flags back
+    # end to end through the public API with host buffers. Headline: swe_step_host,
+    # the step reading the state from pinned host memory and writing the new state
+    # and the flags back to pinned host memory inside the kernel (over the
+    # coherent CPU-GPU link); every step completes (synchronised) before the next.
+    # Also reported: the upload / traverse / download round trip with copies.
     e2e = None
     if not a.no_e2e:
-        pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory().numpy()
-        hh, hu, hv, hb = (pin(x) for x in ctx.download_state())
-        flags = pin(np.zeros(n, np.int8))
-        ctx.traverse(1)
+        hs = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in ctx.download_state()]
+        cur, hb = hs[:3], hs[3]
+        nxt = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(3)]
+        hflags = torch.zeros(n, dtype=torch.int8).pin_memory()
+        ctx.step_host(*cur, hb, *nxt, hflags)  # warm-up
         ctx.synchronize()
+        cur, nxt = nxt, cur
         if world > 1:
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(a.e2e_steps):
-            ctx.upload_state(hh, hu, hv, hb)
-            ctx.traverse(1)
-            ctx.download_state([hh, hu, hv, hb])
-            ctx.refinements(flags)
+            ctx.step_host(*cur, hb, *nxt, hflags)
+            ctx.synchronize()
+            cur, nxt = nxt, cur
         te = time.perf_counter() - t0
+        hh, hu, hv = (t.numpy() for t in cur)
+        flags = hflags.numpy()
+        ctx.upload_state(hh, hu, hv, hb.numpy())
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.e2e_steps):
+            ctx.upload_state(hh, hu, hv, hb.numpy())
+            ctx.traverse(1)
+            ctx.download_state([hh, hu, hv, hb.numpy()])
+            ctx.refinements(flags)
+        tc = time.perf_counter() - t0
         if world > 1:
-            t = torch.tensor([te], device="cuda")
+            t = torch.tensor([te, tc], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
+            te, tc = (float(x) for x in t.tolist())
         e2e = {"value": n * a.e2e_steps * world / te, "unit": UNIT, "h2d_bytes_per_step": 32 * n,
-               "d2h_bytes_per_step": 32 * n + n + 40, "steps": a.e2e_steps,
-               "note": "state upload from pinned host memory + step + state and flags download, every step"}
+               "d2h_bytes_per_step": 24 * n + n, "steps": a.e2e_steps, "api": "swe_step_host",
+               "note": "every step reads h, hu, hv, b from pinned host memory and writes h, hu, hv and the "
+                       "refinement flags to pinned host memory inside the step kernel, then synchronises",
+               "copy_round_trip": {"value": n * a.e2e_steps * world / tc, "h2d_bytes_per_step": 32 * n,
+                                   "d2h_bytes_per_step": 32 * n + n + 40,
+                                   "api": "swe_state_upload + swe_traverse + swe_state_download + "
+                                          "swe_get_refinements"}}
 
     peaks, peak_kind = measured_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -456,7 +487,7 @@ def run_gpu(a, rank, world, local):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "cells": n,
                        "solver": a.solver, "boundary": "outflow", "segment_cells": tiling[0],
-                       "block_threads": tiling[1], "arith": a.arith,
+                       "block_threads": tiling[1], "arith": a.arith, "autotune": tuning,
                        "l2": "inputs larger than L2 (2.1 GB state)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline,

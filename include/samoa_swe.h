@@ -241,6 +241,23 @@ int swe_mesh_validate(int64_t n_cells, const int8_t* depth, const int8_t* plotte
 int swe_riemann_batch(int32_t solver, int64_t n, const double* normals, const double* q_left, const double* q_right,
                       double dry_tolerance, double* out_left, double* out_right);
 
+/* One step on state arrays the caller keeps in host memory (or device memory):
+ * the step reads h, hu, hv and b where they are and writes h_out, hu_out,
+ * hv_out and the refinement flags (flags_out may be NULL: the context's
+ * buffer) directly, with no staging copies; on a Grace-Blackwell node the
+ * kernel streams them over the coherent CPU-GPU link. Replaces the upload /
+ * traverse / download round trip a host that owns the arrays (the Fortran grid)
+ * would otherwise make around swe%euler%traverse (src/SWE/SWE.f90:393). Arrays:
+ * n_cells doubles in the mesh order; pinned (cudaHostAlloc / cudaHostRegister)
+ * or device memory, or pageable memory where the device reads it coherently
+ * (cudaDevAttrPageableMemoryAccess); inputs and outputs must not overlap.
+ * b = NULL uses the uploaded bathymetry. Time, dt, the step counter (traversal
+ * direction) and the refinement count advance as in swe_traverse; the
+ * context's own state buffers are left as they were. Single-instance contexts
+ * only. Returns without synchronising (swe_synchronize before reading). */
+int swe_step_host(swe_ctx* ctx, const double* h, const double* hu, const double* hv, const double* b,
+                  double* h_out, double* hu_out, double* hv_out, int8_t* flags_out);
+
 /* Device self-check of the step's correctly rounded division with a shared
  * reciprocal (the quotients u = hu / h and v = hv / h, which share h, and the
  * two f-wave coefficients, which share s2 - s1): on 2n seeded random pairs

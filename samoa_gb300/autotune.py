@@ -12,7 +12,7 @@ import numpy as np
 
 from . import swe
 
-DEFAULT_SEGMENTS = (256, 384, 512, 768, 1024)
+DEFAULT_SEGMENTS = (256, 384, 448, 512, 640, 768, 1024)
 DEFAULT_THREADS = (128, 256)
 
 

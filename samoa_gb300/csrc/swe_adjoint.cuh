@@ -28,8 +28,8 @@ struct Grad4 {
 // outL / outR. QL / QR are the states (h = surface), dL / dR their depths,
 // sqL0 / sqR0 their sqrt(g * depth) as in the forward step.
 __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL, const State& QR, double dL0,
-                                       double dR0, double sqL0, double sqR0, double drytol, const double gL[3],
-                                       const double gR[3], Grad4& outL, Grad4& outR) {
+                                       double dR0, double sqL0, double sqR0, double yL0, double yR0, double drytol,
+                                       const double gL[3], const double gR[3], Grad4& outL, Grad4& outR) {
     const double g = kG;
     const double c = 0.5 * g;
     // ---------------- forward (geoclaw_flux<FWAVE>, same expressions)
@@ -42,12 +42,14 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const bool wetR = hR > drytol, wetL = hL > drytol;
     double huL, huR, uL, uR, vL, vR;
     if (wetR) {
-        huR = pR1; uR = pR1 / hR; vR = pR2 / hR;
+        const Recip r{hR, yR0, recip_fast(hR)};
+        huR = pR1; uR = div_rn(pR1, r); vR = div_rn(pR2, r);
     } else {
         hR = 0.0; huR = 0.0; uR = 0.0; vR = 0.0;
     }
     if (wetL) {
-        huL = pL1; uL = pL1 / hL; vL = pL2 / hL;
+        const Recip r{hL, yL0, recip_fast(hL)};
+        huL = pL1; uL = div_rn(pL1, r); vL = div_rn(pL2, r);
     } else {
         hL = 0.0; huL = 0.0; uL = 0.0; vL = 0.0;
     }
@@ -80,7 +82,8 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double sqR = (wetR || wall_r) ? (wall_r ? sqL0 : sqR0) : 0.0;
     const double sL = uL - sqL, sR = uR + sqR;
     const double A = sqL * uL + sqR * uR, B = sqR + sqL;
-    const double uhat = A / B;
+    const Recip rB = recip_rn(B);
+    const double uhat = div_rn(A, rB);
     const double chat = sqrt((g * 0.5) * Hs);
     const double r1 = uhat - chat, r2 = uhat + chat;
     const bool e1_is_sL = sL < r1, e2_is_sR = sR > r2;
@@ -91,8 +94,9 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double ddp = -(K * dB);
     const double dpd = delphi - ddp;
     const double D = sE2 - sE1;
-    const double beta1 = (sE2 * delhu - dpd) / D;
-    const double beta2 = (dpd - sE1 * delhu) / D;
+    const Recip rD = recip_rn(D);
+    const double beta1 = div_rn(sE2 * delhu - dpd, rD);
+    const double beta2 = div_rn(dpd - sE1 * delhu, rD);
     const double sw[3] = {sE1, 0.5 * (sE1 + sE2), sE2};
     // ---------------- reverse
     // back-rotation p = net(2:3) T
@@ -119,8 +123,8 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     b_vL += F30 * beta1;
     b_vR += F32 * beta2;
     // beta1 = (sE2 delhu - dpd) / D, beta2 = (dpd - sE1 delhu) / D, D = sE2 - sE1
-    const double N1b = b_beta1 / D, N2b = b_beta2 / D;
-    const double b_D = -(b_beta1 * beta1 + b_beta2 * beta2) / D;
+    const double N1b = b_beta1 * rD.y, N2b = b_beta2 * rD.y;
+    const double b_D = -(b_beta1 * beta1 + b_beta2 * beta2) * rD.y;
     b_sE2 += N1b * delhu + b_D;
     b_sE1 += -N2b * delhu - b_D;
     double b_delhu = N1b * sE2 - N2b * sE1;
@@ -139,10 +143,10 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     double b_sR = e2_is_sR ? b_sE2 : 0.0, b_r2 = e2_is_sR ? 0.0 : b_sE2;
     const double b_uhat = b_r1 + b_r2;
     const double b_chat = b_r2 - b_r1;
-    if (chat > 0.0) b_Hs += b_chat * (0.5 / chat) * (g * 0.5);
+    if (chat > 0.0) b_Hs += b_chat * (0.5 * rcp_nr(chat)) * (g * 0.5);
     double b_uL = b_sL, b_uR = b_sR;
     double b_sqL = -b_sL, b_sqR = b_sR;
-    const double b_A = b_uhat / B, b_B = -b_uhat * uhat / B;
+    const double b_A = b_uhat * rB.y, b_B = -b_uhat * uhat * rB.y;
     b_sqL += b_A * uL + b_B;
     b_sqR += b_A * uR + b_B;
     b_uL += b_A * sqL;
@@ -169,8 +173,8 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         b_bR += b_dB;
         b_bL -= b_dB;
         // sqrt(g h) of the fixed-up depths
-        if (sqL > 0.0) b_hL += b_sqL * (0.5 * g / sqL);
-        if (sqR > 0.0) b_hR += b_sqR * (0.5 * g / sqR);
+        if (sqL > 0.0) b_hL += b_sqL * (0.5 * g * rcp_nr(sqL));
+        if (sqR > 0.0) b_hR += b_sqR * (0.5 * g * rcp_nr(sqR));
         // undo the wall / lowering fix-ups: map the cotangents back to the original sides
         double b_hL0 = 0.0, b_hR0 = 0.0, b_bL0 = 0.0, b_bR0 = 0.0;
         if (wall_r) {  // hR = hL, huR = -huL, bR = bL, uR = -uL, vR = vL
@@ -200,14 +204,14 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         // wet extraction: u = hu / h, v = hv / h on wet sides; dry sides are constants
         double b_pL1 = 0.0, b_pL2 = 0.0, b_pR1 = 0.0, b_pR2 = 0.0;
         if (wetR) {
-            b_pR1 += b_huR + b_uR / hR;
-            b_pR2 += b_vR / hR;
-            b_hR0 = b_hR - (b_uR * uR + b_vR * vR) / hR;
+            b_pR1 += b_huR + b_uR * yR0;
+            b_pR2 += b_vR * yR0;
+            b_hR0 = b_hR - (b_uR * uR + b_vR * vR) * yR0;
         }
         if (wetL) {
-            b_pL1 += b_huL + b_uL / hL;
-            b_pL2 += b_vL / hL;
-            b_hL0 = b_hL - (b_uL * uL + b_vL * vL) / hL;
+            b_pL1 += b_huL + b_uL * yL0;
+            b_pL2 += b_vL * yL0;
+            b_hL0 = b_hL - (b_uL * uL + b_vL * vL) * yL0;
         }
         // depths h - b, rotations p_edge = T p
         outL.h += b_hL0;
@@ -282,8 +286,8 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
     double* sh_hu = sh_h + T;
     double* sh_hv = sh_hu + T;
     double* sh_b = sh_hv + T;
-    double* sh_d = sh_b + T;
-    double* sh_sq = sh_d + T;
+    double* sh_rh = sh_b + T;          // RN(1 / depth) where wet
+    double* sh_sq = sh_rh + T;
     double* sh_mu = sh_sq + T;         // [3][T]
     double* slot = sh_mu + 3 * T;      // [4 quantities][3 local edges][T]
     const InstParams& P = A.P;
@@ -300,9 +304,9 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
             sh_hu[i] = A.hu[cc];
             sh_hv[i] = A.hv[cc];
             sh_b[i] = b;
-            double d, sq;
-            depth_terms(State{h, 0.0, 0.0, b}, P.drytol, d, sq);
-            sh_d[i] = d;
+            double d, sq, y;
+            depth_terms(State{h, 0.0, 0.0, b}, P.drytol, d, sq, y);
+            sh_rh[i] = y;
             sh_sq[i] = sq;
             const int dd = A.depth[cc];
             const double vol = (P.scaling * P.scaling) * c_vol[dd];
@@ -338,16 +342,17 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
             const bool lin = (unsigned)sl < (unsigned)cn;
             const bool rin = !bnd && (unsigned)sr < (unsigned)cn;
             State QL, QR;
-            double dL, dR, sqL, sqR, mL[3], mR[3] = {0.0, 0.0, 0.0};
+            double dL, dR, sqL, sqR, yL, yR, mL[3], mR[3] = {0.0, 0.0, 0.0};
             int depL, depR = 0;
             if (lin) {
                 QL = State{sh_h[sl], sh_hu[sl], sh_hv[sl], sh_b[sl]};
-                dL = sh_d[sl];
+                dL = QL.h - QL.b;
                 sqL = sh_sq[sl];
+                yL = sh_rh[sl];
                 mL[0] = sh_mu[sl]; mL[1] = sh_mu[T + sl]; mL[2] = sh_mu[2 * T + sl];
             } else {
                 QL = State{A.h[L], A.hu[L], A.hv[L], A.b[L]};
-                depth_terms(QL, P.drytol, dL, sqL);
+                depth_terms(QL, P.drytol, dL, sqL, yL);
                 const int dd = A.depth[L];
                 cell_mu(A, L, -A.dt / ((P.scaling * P.scaling) * c_vol[dd]), mL[0], mL[1], mL[2]);
             }
@@ -358,15 +363,17 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                 else QR = QL;
                 dR = dL;
                 sqR = sqL;
+                yR = yL;
             } else {
                 if (rin) {
                     QR = State{sh_h[sr], sh_hu[sr], sh_hv[sr], sh_b[sr]};
-                    dR = sh_d[sr];
+                    dR = QR.h - QR.b;
                     sqR = sh_sq[sr];
+                    yR = sh_rh[sr];
                     mR[0] = sh_mu[sr]; mR[1] = sh_mu[T + sr]; mR[2] = sh_mu[2 * T + sr];
                 } else {
                     QR = State{A.h[R], A.hu[R], A.hv[R], A.b[R]};
-                    depth_terms(QR, P.drytol, dR, sqR);
+                    depth_terms(QR, P.drytol, dR, sqR, yR);
                     const int dd = A.depth[R];
                     cell_mu(A, R, -A.dt / ((P.scaling * P.scaling) * c_vol[dd]), mR[0], mR[1], mR[2]);
                 }
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                 gR[2] = lenR * mR[2];
             }
             Grad4 oL{0.0, 0.0, 0.0, 0.0}, oR{0.0, 0.0, 0.0, 0.0};
-            fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, P.drytol, gL, gR, oL, oR);
+            fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR);
             if (bnd) {  // the ghost's cotangent goes back to the cell
                 if (P.bc == BC_SLIP) boundary_ghost_vjp<BC_SLIP>(n1, n2, oR, oL);
                 else if (P.bc == BC_NOSLIP) boundary_ghost_vjp<BC_NOSLIP>(n1, n2, oR, oL);

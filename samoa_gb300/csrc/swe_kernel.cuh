@@ -63,6 +63,7 @@ struct StepArgs {
     long long dt_seq_len;      // steps in the sequence
     int32_t n_seg, n_inst, seg_cells, max_ndepth, n_cells_total;
     int32_t use_tma;
+    int32_t fixed_io;          // 1: read h[0], hu[0], hv[0] and write h[1].. on every step (caller's buffers)
 };
 
 constexpr int kWaitLimit = 1 << 24;  // polls of an mbarrier before a kernel gives up
@@ -198,12 +199,13 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
     const long long step = A.gs->step;
     const long long kseq = step - A.gs->dt_seq_base;
     const int odd = (int)(step & 1);
-    const double* hin = A.h[odd];
-    const double* huin = A.hu[odd];
-    const double* hvin = A.hv[odd];
-    double* hout = A.h[odd ^ 1];
-    double* huout = A.hu[odd ^ 1];
-    double* hvout = A.hv[odd ^ 1];
+    const int ib = A.fixed_io ? 0 : odd;
+    const double* hin = A.h[ib];
+    const double* huin = A.hu[ib];
+    const double* hvin = A.hv[ib];
+    double* hout = A.h[ib ^ 1];
+    double* huout = A.hu[ib ^ 1];
+    double* hvout = A.hv[ib ^ 1];
 
     if (tid == 0) {
         s_error = 0;

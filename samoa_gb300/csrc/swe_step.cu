@@ -455,7 +455,10 @@ int copy_state(swe_ctx* c, int to_device, double* h, double* hu, double* hv, dou
     return SWE_OK;
 }
 
-int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr) {
+// io: optional caller buffers {h, hu, hv, h_out, hu_out, hv_out} (device-accessible
+// addresses), b and flags: optional replacements of the context's arrays.
+int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double* const* io = nullptr,
+                 const double* b = nullptr, int8_t* flags = nullptr, int use_tma = 1) {
     StepArgs A;
     A.branch = branch;
     for (int k = 0; k < 2; ++k) {
@@ -479,7 +482,15 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr) {
     A.seg_cells = c->seg_cells;
     A.max_ndepth = c->max_ndepth;
     A.n_cells_total = (int32_t)c->cells_total;
-    A.use_tma = 1;
+    A.use_tma = use_tma;
+    A.fixed_io = 0;
+    if (io) {
+        A.h[0] = io[0]; A.hu[0] = io[1]; A.hv[0] = io[2];
+        A.h[1] = io[3]; A.hu[1] = io[4]; A.hv[1] = io[5];
+        A.fixed_io = 1;
+    }
+    if (b) A.b = b;
+    if (flags) A.flags = flags;
     // the adjoint's forward step (branch output) always runs the strict kernel,
     // so its branches are the ones the reverse sweep re-evaluates
     void* k = (c->arith == SWE_ARITH_FMA && !branch) ? fma_step_kernel(c->params[0].solver)
@@ -743,6 +754,82 @@ int swe_traverse(swe_ctx* c, int64_t n_steps) {
     if (n_steps < 0) return set_error(SWE_E_INVALID, "n_steps < 0");
     cudaSetDevice(c->device);
     return launch_steps(c, n_steps);
+}
+
+}  // extern "C"
+
+namespace {
+// The address the device uses for a caller's array: device or managed memory
+// as is, pinned host memory through its device alias, pageable host memory
+// only where the device reads it coherently (pageable memory access).
+int device_view(const swe_ctx* c, const void* p, const char* name, const void** out, bool* on_device) {
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(SWE_E_INVALID, "%s: cannot query the pointer (%s)", name, cudaGetErrorString(e));
+    }
+    *on_device = false;
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        if (at.type == cudaMemoryTypeDevice && at.device != c->device)
+            return set_error(SWE_E_INVALID, "%s is memory of device %d, the context runs on %d", name, at.device,
+                             c->device);
+        *out = p;
+        *on_device = at.type == cudaMemoryTypeDevice;
+        return SWE_OK;
+    }
+    if (at.type == cudaMemoryTypeHost) {
+        if (!at.devicePointer) return set_error(SWE_E_INVALID, "%s: pinned memory without a device mapping", name);
+        *out = at.devicePointer;
+        return SWE_OK;
+    }
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device);
+    if (!pageable)
+        return set_error(SWE_E_INVALID, "%s is pageable host memory and device %d cannot read it; pin it "
+                         "(cudaHostRegister) or pass device memory", name, c->device);
+    *out = p;
+    return SWE_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int swe_step_host(swe_ctx* c, const double* h, const double* hu, const double* hv, const double* b, double* h_out,
+                  double* hu_out, double* hv_out, int8_t* flags_out) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (!c->has_mesh) return set_error(SWE_E_NOMESH, "upload a mesh first");
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "swe_step_host takes a single-instance context");
+    if (!h || !hu || !hv || !h_out || !hu_out || !hv_out) return set_error(SWE_E_INVALID, "null state array");
+    if (!b && !c->has_state) return set_error(SWE_E_STATE, "b = NULL needs an uploaded state (its bathymetry)");
+    const int64_t n = c->mesh[0].n_cells;
+    const double* in[3] = {h, hu, hv};
+    const double* out[3] = {h_out, hu_out, hv_out};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (in[i] < out[j] + n && out[j] < in[i] + n)
+                return set_error(SWE_E_INVALID, "input and output arrays overlap");
+    cudaSetDevice(c->device);
+    const char* names[8] = {"h", "hu", "hv", "h_out", "hu_out", "hv_out", "b", "flags_out"};
+    const void* dv[8] = {nullptr};
+    const void* src[8] = {h, hu, hv, h_out, hu_out, hv_out, b, flags_out};
+    bool all_dev = true;
+    for (int i = 0; i < 8; ++i) {
+        if (!src[i]) continue;
+        bool od = false;
+        int rc = device_view(c, src[i], names[i], &dv[i], &od);
+        if (rc) return rc;
+        all_dev = all_dev && od;
+    }
+    double* io[6];
+    for (int i = 0; i < 6; ++i) io[i] = const_cast<double*>(static_cast<const double*>(dv[i]));
+    // the 1-D bulk copies stage device memory from 16-byte aligned bases (every
+    // segment starts at an even cell); host memory is read with plain loads
+    bool aligned = true;
+    for (int i = 0; i < 3; ++i) aligned = aligned && ((uintptr_t)dv[i] & 15u) == 0;
+    aligned = aligned && (!dv[6] || ((uintptr_t)dv[6] & 15u) == 0) && (dv[6] || c->b);
+    return launch_steps(c, 1, nullptr, io, static_cast<const double*>(dv[6]),
+                        static_cast<int8_t*>(const_cast<void*>(dv[7])), (all_dev && aligned) ? 1 : 0);
 }
 
 int swe_traverse_graph(swe_ctx* c, int64_t n_steps) {

@@ -181,6 +181,17 @@ class SweContext:
     def traverse(self, n_steps=1):
         _lib.check(self.L.swe_traverse(self.ptr, int(n_steps)))
 
+    def step_host(self, h, hu, hv, b, h_out, hu_out, hv_out, flags_out=None):
+        """One step reading (h, hu, hv, b) and writing (h_out, hu_out, hv_out,
+        flags_out) where they live: torch tensors in pinned host memory or on
+        the context's device (b and flags_out may be None). Asynchronous."""
+        ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+        for t in (h, hu, hv, b, h_out, hu_out, hv_out, flags_out):
+            if t is not None and (not t.is_contiguous() or t.numel() < self.n_cells):
+                raise ValueError("arrays must be contiguous with n_cells elements")
+        _lib.check(self.L.swe_step_host(self.ptr, ptr(h), ptr(hu), ptr(hv), ptr(b), ptr(h_out), ptr(hu_out),
+                                        ptr(hv_out), ptr(flags_out)))
+
     def refinements(self, flags=None):
         if flags is None:
             flags = np.empty(self.n_cells, np.int8)

@@ -1,0 +1,95 @@
+"""swe_step_host: the step reading and writing the caller's arrays in pinned
+host memory (or device memory) equals the resident-state step bit for bit,
+including the refinement flags, the dt and the traversal direction."""
+import numpy as np
+import pytest
+
+from samoa_gb300 import scenarios, swe
+
+pytestmark = pytest.mark.gpu
+
+
+def _dt0(scn):
+    g = scn.grid
+    return swe.initial_dt(g.mesh, g.h, g.hu, g.hv, g.b, scn.cfg.courant_number)
+
+
+def _resident(scn, steps):
+    ctx = swe.SweContext(0)
+    try:
+        ctx.set_params(scn.cfg.params())
+        ctx.upload_mesh(scn.grid.mesh)
+        g = scn.grid
+        ctx.upload_state(g.h, g.hu, g.hv, g.b)
+        ctx.set_time(0.0, _dt0(scn))
+        out = []
+        for _ in range(steps):
+            ctx.traverse(1)
+            h, hu, hv, _ = ctx.download_state()
+            flags, n = ctx.refinements()
+            out.append((h, hu, hv, flags.copy(), n, ctx.get_time()))
+        return out
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("where", ["pinned", "device", "device_offset"])
+def test_host_step_matches_resident_step(swe_lib, where):
+    import torch
+    scn = scenarios.radial_dam_break(log2_cells=12, boundary="slip")
+    g = scn.grid
+    steps = 3
+    ref = _resident(scn, steps)
+    n = g.mesh.n_cells
+    if where == "pinned":
+        mk = lambda a: torch.tensor(a).pin_memory()
+        buf = lambda dt: torch.zeros(n, dtype=dt).pin_memory()
+    elif where == "device":
+        mk = lambda a: torch.tensor(a, device="cuda")
+        buf = lambda dt: torch.zeros(n, dtype=dt, device="cuda")
+    else:  # 8-byte aligned bases: the plain-load staging path
+        mk = lambda a: torch.tensor(np.concatenate([[0.0], a]), device="cuda")[1:]
+        buf = lambda dt: torch.zeros(n + 1, dtype=dt, device="cuda")[1:]
+    cur = [mk(g.h), mk(g.hu), mk(g.hv)]
+    nxt = [buf(torch.float64) for _ in range(3)]
+    b = mk(g.b)
+    flags = buf(torch.int8)
+    ctx = swe.SweContext(0)
+    try:
+        ctx.set_params(scn.cfg.params())
+        ctx.upload_mesh(g.mesh)
+        ctx.set_time(0.0, _dt0(scn))
+        for k in range(steps):
+            ctx.step_host(*cur, b, *nxt, flags)
+            ctx.synchronize()
+            h, hu, hv, f, nref, tm = ref[k]
+            assert np.array_equal(nxt[0].cpu().numpy(), h)
+            assert np.array_equal(nxt[1].cpu().numpy(), hu)
+            assert np.array_equal(nxt[2].cpu().numpy(), hv)
+            assert np.array_equal(flags.cpu().numpy(), f)
+            assert ctx.get_time() == tm
+            cur, nxt = nxt, cur
+    finally:
+        ctx.close()
+
+
+def test_host_step_rejects_overlap_and_pageable_policy(swe_lib):
+    import torch
+    from samoa_gb300 import _lib
+    scn = scenarios.radial_dam_break(log2_cells=10, boundary="outflow")
+    g = scn.grid
+    n = g.mesh.n_cells
+    ctx = swe.SweContext(0)
+    try:
+        ctx.set_params(scn.cfg.params())
+        ctx.upload_mesh(g.mesh)
+        ctx.set_time(0.0, _dt0(scn))
+        a = torch.zeros(4 * n, dtype=torch.float64).pin_memory()
+        b = torch.tensor(g.b).pin_memory()
+        with pytest.raises(_lib.SweError):  # h_out overlaps h and hu
+            ctx.step_host(a[:n], a[n:2 * n], a[2 * n:3 * n], b, a[n // 2:n // 2 + n], a[3 * n:], a[3 * n:])
+        with pytest.raises(_lib.SweError):  # no bathymetry anywhere
+            ctx.step_host(a[:n], a[n:2 * n], a[2 * n:3 * n], None, *[torch.zeros(n, dtype=torch.float64).pin_memory()
+                                                                    for _ in range(3)])
+    finally:
+        ctx.close()
