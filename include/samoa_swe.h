@@ -227,6 +227,24 @@ int swe_step_back(swe_ctx* ctx);
 int swe_adjoint_step(swe_ctx* ctx, const uint8_t* branch, const double* lam_h, const double* lam_hu,
                      const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar);
 
+/* Gradient of the gauge misfit J = sum_t sum_g (h_{t+1}[gauges[g]] - obs[t][g])^2
+ * over n_steps f-wave steps with the frozen dt sequence dts (host, n_steps),
+ * from the context's current state x_0, by one checkpointed reverse sweep run
+ * entirely in the library: binomial checkpointing (revolve's offline schedule)
+ * with `snapshots` device snapshot slots, each forward step recording its
+ * branches, the first visit of each step sampling the gauges, each reverse step
+ * adding the gauge residuals and calling the step's discrete adjoint. Device
+ * arrays: gauges[n_gauges] (cells), obs[n_steps * n_gauges]; outputs
+ * gauge_values[n_steps * n_gauges] (may be NULL), grad_h (dJ/dh of x_0),
+ * grad_hu, grad_hv (may be NULL), grad_b (dJ/db); J and forward_steps (may be
+ * NULL) on the host. The context is left at x_0 and its step count; the dt
+ * sequence stays set. Synchronises before returning. Allocates
+ * snapshots * 24 * n_cells + n_steps * n_cells bytes for the sweep.
+ * No counterpart in the reference. */
+int swe_gauge_gradient(swe_ctx* ctx, int64_t n_steps, const double* dts, int32_t snapshots, int64_t n_gauges,
+                       const int64_t* gauges, const double* obs, double* gauge_values, double* grad_h,
+                       double* grad_hu, double* grad_hv, double* grad_b, double* J, int64_t* forward_steps);
+
 /* Check a mesh in the swe_mesh_upload layout on the host without a context
  * (same checks as the upload): 0 if valid, SWE_E_INVALID with a message otherwise. */
 int swe_mesh_validate(int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,

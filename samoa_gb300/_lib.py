@@ -22,7 +22,7 @@ EXPORTS = [
     "swe_ensemble_set_params", "swe_ensemble_set_time", "swe_ensemble_get_time", "swe_ensemble_get_refinements",
     "swe_traverse_graph", "swe_set_dt_sequence", "swe_step_noalloc", "swe_snapshot_store", "swe_snapshot_restore",
     "swe_sample_gauges", "swe_adjoint_step", "swe_set_arith", "swe_traverse_branches", "swe_step_back",
-    "swe_division_check", "swe_step_host",
+    "swe_division_check", "swe_step_host", "swe_gauge_gradient",
 ]
 
 
@@ -89,6 +89,7 @@ def load():
         "swe_set_arith": [P, i32],
         "swe_division_check": [i64, C.c_uint64, i32, P],
         "swe_step_host": [P, P, P, P, P, P, P, P, P],
+        "swe_gauge_gradient": [P, i64, P, i32, i64, P, P, P, P, P, P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

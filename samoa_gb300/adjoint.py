@@ -166,9 +166,31 @@ class GaugeProblem:
         return J
 
     def gradient(self, h0, b):
-        """(J, dJ/dh0, dJ/db) from one checkpointed sweep: the first forward
-        descent of the schedule records the gauges (for J and its residuals) and
-        every forward step records its branches for the reverse step."""
+        """(J, dJ/dh0, dJ/db) from one checkpointed sweep run inside the library
+        (swe_gauge_gradient: the same schedule as gradient_python, no host round
+        trips between steps)."""
+        self._set_initial(h0, b)
+        L = self.ctx.L
+        with torch.cuda.stream(self.stream):
+            self.gv = torch.empty((self.T, len(self.gauges)), dtype=torch.float64, device=self.dev)
+            gh = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+            gb = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+        self.stream.synchronize()
+        J = C.c_double()
+        fwd = C.c_int64()
+        _lib.check(L.swe_gauge_gradient(self.ctx.ptr, self.T, self.dts.ctypes.data_as(C.c_void_p), self.snapshots,
+                                        len(self.gauges), _vp(self.gauges), _vp(self.obs), _vp(self.gv), _vp(gh),
+                                        None, None, _vp(gb), C.byref(J), C.byref(fwd)))
+        self.stats["forward_steps"] += fwd.value
+        self.stats["adjoint_steps"] += self.T
+        self.gauge_values = self.gv
+        return J.value, gh, gb
+
+    def gradient_python(self, h0, b):
+        """(J, dJ/dh0, dJ/db) from one checkpointed sweep driven from Python step
+        by step: the first forward descent of the schedule records the gauges
+        (for J and its residuals) and every forward step records its branches
+        for the reverse step."""
         n = self.n
         L = self.ctx.L
         problem = self

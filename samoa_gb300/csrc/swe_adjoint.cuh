@@ -27,19 +27,34 @@ struct Grad4 {
 // net updates (h, hu, hv, world frame), add the cotangents of the inputs to
 // outL / outR. QL / QR are the states (h = surface), dL / dR their depths,
 // sqL0 / sqR0 their sqrt(g * depth) as in the forward step.
+// axis: the normal's direction as in geoclaw_flux (0 diagonal, 1 along x, 2 along y).
 __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL, const State& QR, double dL0,
                                        double dR0, double sqL0, double sqR0, double yL0, double yR0, double drytol,
-                                       const double gL[3], const double gR[3], Grad4& outL, Grad4& outR) {
+                                       const double gL[3], const double gR[3], Grad4& outL, Grad4& outR,
+                                       int axis = 0) {
     const double g = kG;
     const double c = 0.5 * g;
-    // ---------------- forward (geoclaw_flux<FWAVE>, same expressions)
-    const double pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
-    const double pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
-    const double pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
-    const double pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+    // ---------------- forward (geoclaw_flux<FWAVE>, the same values)
+    const bool fast = axis != 0 && is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
+    const bool sn = axis == 1 ? lt0(n1) : lt0(n2);
+    double pL1, pL2, pR1, pR2;
+    if (fast) {
+        if (axis == 1) {
+            pL1 = z0(flip(QL.p1, sn)); pL2 = z0(flip(QL.p2, sn));
+            pR1 = z0(flip(QR.p1, sn)); pR2 = z0(flip(QR.p2, sn));
+        } else {
+            pL1 = z0(flip(QL.p2, sn)); pL2 = z0(flip(QL.p1, !sn));
+            pR1 = z0(flip(QR.p2, sn)); pR2 = z0(flip(QR.p1, !sn));
+        }
+    } else {
+        pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
+        pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
+        pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
+        pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+    }
     double hL = dL0, hR = dR0, bL = QL.b, bR = QR.b;
-    if (hL <= drytol && hR <= drytol) return;  // no flux, no derivative
-    const bool wetR = hR > drytol, wetL = hL > drytol;
+    const bool wetR = lt(drytol, hR), wetL = lt(drytol, hL);
+    if (!wetL && !wetR && !is_nan(hL) && !is_nan(hR)) return;  // no flux, no derivative
     double huL, huR, uL, uR, vL, vR;
     if (wetR) {
         const Recip r{hR, yR0, recip_fast(hR)};
@@ -86,7 +101,7 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double uhat = div_rn(A, rB);
     const double chat = sqrt((g * 0.5) * Hs);
     const double r1 = uhat - chat, r2 = uhat + chat;
-    const bool e1_is_sL = sL < r1, e2_is_sR = sR > r2;
+    const bool e1_is_sL = lt(sL, r1), e2_is_sR = lt(r2, sR);
     const double sE1 = e1_is_sL ? sL : r1, sE2 = e2_is_sR ? sR : r2;
     const double delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) + ((c * X) * Hs)) - ((c * Hs) * dB);
     const double delhu = huR - huL;
@@ -99,15 +114,26 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double beta2 = div_rn(dpd - sE1 * delhu, rD);
     const double sw[3] = {sE1, 0.5 * (sE1 + sE2), sE2};
     // ---------------- reverse
-    // back-rotation p = net(2:3) T
-    double nL[3] = {gL[0], gL[1] * n1 + gL[2] * n2, -gL[1] * n2 + gL[2] * n1};
-    double nR[3] = {gR[0], gR[1] * n1 + gR[2] * n2, -gR[1] * n2 + gR[2] * n1};
+    // back-rotation p = net(2:3) T (for an axis-aligned normal: signed selections)
+    double nL[3], nR[3];
+    nL[0] = gL[0];
+    nR[0] = gR[0];
+    if (axis == 1) {
+        nL[1] = flip(gL[1], sn); nL[2] = flip(gL[2], sn);
+        nR[1] = flip(gR[1], sn); nR[2] = flip(gR[2], sn);
+    } else if (axis == 2) {
+        nL[1] = flip(gL[2], sn); nL[2] = flip(gL[1], !sn);
+        nR[1] = flip(gR[2], sn); nR[2] = flip(gR[1], !sn);
+    } else {
+        nL[1] = gL[1] * n1 + gL[2] * n2; nL[2] = -gL[1] * n2 + gL[2] * n1;
+        nR[1] = gR[1] * n1 + gR[2] * n2; nR[2] = -gR[1] * n2 + gR[2] * n1;
+    }
     // net-update split by wave-speed sign; walls remove waves
     double F[3][3];
 #pragma unroll
     for (int w = 0; w < 3; ++w) {
         const bool zeroed = (wall_l && w < 2) || (wall_r && w > 0);
-        const bool neg = sw[w] < 0.0, pos = sw[w] > 0.0;
+        const bool neg = lt0(sw[w]), pos = gt0(sw[w]);
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
             double f = neg ? nL[e] : (pos ? nR[e] : 0.5 * (nL[e] + nR[e]));
@@ -218,10 +244,18 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         outL.b += b_bL0 - b_hL0;
         outR.h += b_hR0;
         outR.b += b_bR0 - b_hR0;
-        outL.hu += b_pL1 * n1 - b_pL2 * n2;
-        outL.hv += b_pL1 * n2 + b_pL2 * n1;
-        outR.hu += b_pR1 * n1 - b_pR2 * n2;
-        outR.hv += b_pR1 * n2 + b_pR2 * n1;
+        if (axis == 1) {
+            outL.hu += flip(b_pL1, sn); outL.hv += flip(b_pL2, sn);
+            outR.hu += flip(b_pR1, sn); outR.hv += flip(b_pR2, sn);
+        } else if (axis == 2) {
+            outL.hu += flip(b_pL2, !sn); outL.hv += flip(b_pL1, sn);
+            outR.hu += flip(b_pR2, !sn); outR.hv += flip(b_pR1, sn);
+        } else {
+            outL.hu += b_pL1 * n1 - b_pL2 * n2;
+            outL.hv += b_pL1 * n2 + b_pL2 * n1;
+            outR.hu += b_pR1 * n1 - b_pR2 * n2;
+            outR.hv += b_pR1 * n2 + b_pR2 * n1;
+        }
     }
 }
 
@@ -390,7 +424,7 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                 gR[2] = lenR * mR[2];
             }
             Grad4 oL{0.0, 0.0, 0.0, 0.0}, oR{0.0, 0.0, 0.0, 0.0};
-            fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR);
+            fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR, (int)((meta >> 15) & 3u));
             if (bnd) {  // the ghost's cotangent goes back to the cell
                 if (P.bc == BC_SLIP) boundary_ghost_vjp<BC_SLIP>(n1, n2, oR, oL);
                 else if (P.bc == BC_NOSLIP) boundary_ghost_vjp<BC_NOSLIP>(n1, n2, oR, oL);

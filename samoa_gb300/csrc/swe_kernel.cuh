@@ -368,10 +368,10 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             ds = ds + leg * upd[(3 * 3 + k2) * T + i];
             int8_t f = 0;
             const double nrm = fabs(dh);
-            if (d < P.max_depth && nrm > P.thr_refine) {
+            if (d < P.max_depth && lt(P.thr_refine, nrm)) {
                 f = 1;
                 ++nref;
-            } else if (d > P.min_depth && nrm < P.thr_coarsen) {
+            } else if (d > P.min_depth && lt(nrm, P.thr_coarsen)) {
                 f = -1;
             }
             if (P.dt_by_max) {  // ds >= 0, so its bits order like its value
@@ -386,8 +386,9 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             double h = sh_h[i], p1 = sh_hu[i], p2 = sh_hv[i];
             const double b = sh_b[i];
             uint8_t br = 0;
-            if (h < b + P.drytol && dh > 0.0) {  // flooded land starts at the dry tolerance, at rest
-                h = b + P.drytol;
+            const double bdry = b + P.drytol;
+            if (lt(h, bdry) && gt0(dh)) {  // flooded land starts at the dry tolerance, at rest
+                h = bdry;
                 p1 = 0.0;
                 p2 = 0.0;
                 br = 1;
@@ -395,8 +396,8 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             h = h + dh;
             p1 = p1 + dp1;
             p2 = p2 + dp2;
-            if (h < b + P.drytol) {  // dried out: surface to min(b, 0), at rest
-                h = dmn(b, 0.0);
+            if (lt(h, bdry)) {  // dried out: surface to min(b, 0), at rest
+                h = lt0(b) ? b : 0.0;
                 p1 = 0.0;
                 p2 = 0.0;
                 br |= 2;

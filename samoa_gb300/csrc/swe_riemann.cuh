@@ -54,6 +54,18 @@ __device__ __forceinline__ bool gt0(double x) {  // x > 0.0
     const long long b = __double_as_longlong(x);
     return b > 0 && b <= 0x7ff0000000000000LL;
 }
+__device__ __forceinline__ bool is_nan(double x) { return abs_bits(x) > 0x7ff0000000000000LL; }
+// A key that orders like the value for non-NaN doubles, with -0 equal to +0.
+__device__ __forceinline__ long long ord_key(double x) {
+    long long b = __double_as_longlong(x);
+    b = (b == (long long)0x8000000000000000ULL) ? 0LL : b;
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool lt(double a, double b) {  // a < b
+    return !is_nan(a) && !is_nan(b) && ord_key(a) < ord_key(b);
+}
+__device__ __forceinline__ double imin(double a, double b) { return lt(a, b) ? a : b; }  // dmn on the integer pipe
+__device__ __forceinline__ double imax(double a, double b) { return lt(b, a) ? a : b; }  // dmx on the integer pipe
 // x with its sign flipped when `neg` (exact, like multiplying by -1)
 __device__ __forceinline__ double flip(double x, bool neg) {
     return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
@@ -283,16 +295,17 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     netL[0] = netL[1] = netL[2] = 0.0;
     netR[0] = netR[1] = netR[2] = 0.0;
     maxspeed = 0.0;
-    if (hL <= drytol && hR <= drytol) return;
+    const bool wetR0 = lt(drytol, hR), wetL0 = lt(drytol, hL);  // h > drytol
+    if (!wetL0 && !wetR0 && !is_nan(hL) && !is_nan(hR) && !is_nan(drytol)) return;  // both h <= drytol
     double uL, uR, vL, vR;
-    if (hR > drytol) {
+    if (wetR0) {
         const Recip r{hR, yR0, recip_fast(hR)};
         uR = div_rn(huR, r);
         vR = div_rn(hvR, r);
     } else {
         hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0;
     }
-    if (hL > drytol) {
+    if (wetL0) {
         const Recip r{hL, yL0, recip_fast(hL)};
         uL = div_rn(huL, r);
         vL = div_rn(hvL, r);
@@ -300,7 +313,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0;
     }
     bool wall_l = false, wall_r = false;  // wall(1) = 0 resp. wall(3) = 0 (wall(2) = 0 with either)
-    if (hR <= drytol) {
+    if (!wetR0) {  // hR is now 0.0, and 0.0 <= drytol
         double hstar, s1m, s2m;
         riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);
         double hstartest = dmx(hL, hstar);
@@ -310,7 +323,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         } else if (hL + bL < bR) {
             bR = hL + bL;
         }
-    } else if (hL <= drytol) {
+    } else if (!wetL0) {
         double hstar, s1m, s2m;
         riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);
         double hstartest = dmx(hR, hstar);
@@ -326,15 +339,16 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
                     (((0.5 * g) * (hR + hL)) * (bR - bL));
     // sqrt(g * h) after the wet/dry fix-ups: a wet side keeps its depth, a dry one
     // has depth 0, and a wall mirrors the wet side's depth
-    const bool wetL = hL > drytol || wall_l, wetR = hR > drytol || wall_r;
+    // a dry side has h = 0 <= drytol now, a wet one is unchanged, a wall mirrors the wet side
+    const bool wetL = wetL0 || wall_l, wetR = wetR0 || wall_r;
     double sqL = wetL ? (wall_l ? sqR0 : sqL0) : 0.0;
     double sqR = wetR ? (wall_r ? sqL0 : sqR0) : 0.0;
     double sL = uL - sqL;
     double sR = uR + sqR;
     double uhat = div_rn(sqL * uL + sqR * uR, recip_rn(sqR + sqL));
     double chat = sqrt((g * 0.5) * (hR + hL));
-    double sE1 = dmn(sL, uhat - chat);
-    double sE2 = dmx(sR, uhat + chat);
+    double sE1 = imin(sL, uhat - chat);
+    double sE2 = imax(sR, uhat + chat);
 
     double sw[3], fw[3][3];
     if (SOLVER == AUG_RIEMANN) {
@@ -543,7 +557,7 @@ __device__ __forceinline__ void depth_terms(const State& Q, double drytol, doubl
 
 __device__ __forceinline__ void depth_terms(const State& Q, double drytol, double& d, double& sq, double& y) {
     d = Q.h - Q.b;
-    const bool wet = d > drytol;
+    const bool wet = lt(drytol, d);
     sq = wet ? sqrt(kG * d) : 0.0;
     y = wet ? recip_rn(d).y : 0.0;
 }

@@ -141,6 +141,32 @@ __global__ void gauge_kernel(const GlobalScalars* G, const double* h0, const dou
     }
 }
 
+// lam_h[gauge g] += 2 (value[g] - obs[g]) for the gauges in order (one thread:
+// a gauge listed twice adds twice, as in sequence)
+__global__ void gauge_residual_kernel(double* lam_h, const int64_t* cells, int64_t n, const double* value,
+                                      const double* obs) {
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (int64_t i = 0; i < n; ++i) lam_h[cells[i]] += 2.0 * (value[i] - obs[i]);
+}
+
+// J = sum over all entries of (value - obs)^2, one block, fixed order per thread
+// then a fixed tree: deterministic from run to run
+__global__ void misfit_kernel(const double* value, const double* obs, int64_t n, double* J) {
+    __shared__ double part[256];
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double r = value[i] - obs[i];
+        acc += r * r;
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *J = part[0];
+}
+
 typedef void (*StepKernel)(StepArgs);
 
 static StepKernel kernel_for(int solver) {
@@ -208,6 +234,14 @@ struct swe_ctx {
     int64_t dt_seq_len = 0;
     std::vector<double> dt_seq_host;
     uint8_t* branch = nullptr;      // wet/dry branch flags of the last forward step (adjoint)
+    // host mirror of the device step counter and dt-sequence base: every change
+    // goes through this library (launches, graph replays, restores), so the host
+    // knows the traversal parity without reading the device
+    long long step_mirror = 0, seq_base_mirror = 0;
+    bool capturing = false;
+    std::vector<InstParams> ip_host;
+    int adj_grid = 0;               // adjoint launch shape for the current tiling (0 = not configured)
+    int32_t adj_seg_cells = 0;
     // CUDA graphs of n steps
     std::map<int64_t, cudaGraphExec_t> graphs;
     double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
@@ -286,6 +320,7 @@ int upload_inst_params(swe_ctx* c) {
         q.dt_by_max = (std::isfinite(v0) && v0 > 0.0 && std::ldexp(v0, -(dmax + 1)) >= DBL_MIN) ? 1 : 0;
     }
     CUDA_TRY(cudaMemcpyAsync(c->ip, v.data(), sizeof(InstParams) * v.size(), cudaMemcpyHostToDevice, c->stream));
+    c->ip_host = v;
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return SWE_OK;
 }
@@ -324,6 +359,7 @@ int rebuild_tasks(swe_ctx* c) {
     c->seg_ptr = nullptr;
     c->seg_info = nullptr;
     c->n_seg = (int64_t)seg_info.size();
+    c->adj_seg_cells = 0;  // the adjoint's grid depends on the segment count
     c->n_tasks = (int64_t)tasks.size();
     if (c->n_seg >= ((int64_t)1 << 31)) return set_error(SWE_E_INVALID, "too many segments");
     int rc;
@@ -350,10 +386,7 @@ int check_device_error(swe_ctx* c) {
 }
 
 int current_index(swe_ctx* c, int* idx) {
-    long long step = 0;
-    CUDA_TRY(cudaMemcpyAsync(&step, &c->gs->step, sizeof(step), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
-    *idx = (int)(step & 1);
+    *idx = (int)(c->step_mirror & 1);
     return SWE_OK;
 }
 
@@ -429,6 +462,8 @@ int upload_meshes(swe_ctx* c, int64_t ni, const int64_t* n_cells, const int64_t*
     reset_scalars_kernel<<<(int)((ni + 255) / 256), 256, 0, c->stream>>>(c->is, c->gs, (int)ni);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->step_mirror = 0;
+    c->seq_base_mirror = 0;
     return SWE_OK;
 }
 
@@ -496,8 +531,10 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     void* k = (c->arith == SWE_ARITH_FMA && !branch) ? fma_step_kernel(c->params[0].solver)
                                                      : (void*)kernel_for(c->params[0].solver);
     void* args[] = {&A};
-    for (int64_t s = 0; s < n_steps; ++s)
+    for (int64_t s = 0; s < n_steps; ++s) {
         CUDA_TRY(cudaLaunchKernel(k, dim3(c->grid), dim3(c->block_threads), args, c->smem, c->stream));
+        if (!c->capturing) ++c->step_mirror;
+    }
     return SWE_OK;
 }
 
@@ -842,7 +879,9 @@ int swe_traverse_graph(swe_ctx* c, int64_t n_steps) {
     if (it == c->graphs.end()) {
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        c->capturing = true;
         rc = launch_steps(c, n_steps);
+        c->capturing = false;
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -856,6 +895,7 @@ int swe_traverse_graph(swe_ctx* c, int64_t n_steps) {
         it = c->graphs.emplace(n_steps, x).first;
     }
     CUDA_TRY(cudaGraphLaunch(it->second, c->stream));
+    c->step_mirror += n_steps;
     return SWE_OK;
 }
 
@@ -878,6 +918,7 @@ int swe_set_dt_sequence(swe_ctx* c, int64_t n_steps, const double* dts) {
     mark_seq_base_kernel<<<1, 1, 0, c->stream>>>(c->gs);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->seq_base_mirror = c->step_mirror;
     c->dt_seq_len = n_steps;
     return SWE_OK;
 }
@@ -888,9 +929,7 @@ int swe_snapshot_store(swe_ctx* c, double* h, double* hu, double* hv, int64_t* s
     if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "snapshots are for single-instance contexts");
     if (!h || !hu || !hv) return set_error(SWE_E_INVALID, "null snapshot buffer");
     cudaSetDevice(c->device);
-    long long s = 0;
-    CUDA_TRY(cudaMemcpyAsync(&s, &c->gs->step, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const long long s = c->step_mirror;
     const int k = (int)(s & 1);
     const size_t bytes = (size_t)c->mesh[0].n_cells * 8;
     CUDA_TRY(cudaMemcpyAsync(h, c->h[k], bytes, cudaMemcpyDeviceToDevice, c->stream));
@@ -913,6 +952,7 @@ int swe_snapshot_restore(swe_ctx* c, const double* h, const double* hu, const do
     CUDA_TRY(cudaMemcpyAsync(c->hv[k], hv, bytes, cudaMemcpyDeviceToDevice, c->stream));
     set_step_kernel<<<1, 1, 0, c->stream>>>(c->gs, (long long)step);
     CUDA_TRY(cudaGetLastError());
+    c->step_mirror = step;
     c->has_state = true;
     return SWE_OK;
 }
@@ -945,37 +985,21 @@ int swe_step_back(swe_ctx* c) {
     if (!c) return set_error(SWE_E_INVALID, "null context");
     if (!c->has_mesh) return set_error(SWE_E_NOMESH, "upload a mesh first");
     cudaSetDevice(c->device);
-    long long s = 0;
-    CUDA_TRY(cudaMemcpyAsync(&s, &c->gs->step, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const long long s = c->step_mirror;
     if (s < 1) return set_error(SWE_E_STATE, "no step to go back from");
     set_step_kernel<<<1, 1, 0, c->stream>>>(c->gs, s - 1);
     CUDA_TRY(cudaGetLastError());
+    c->step_mirror = s - 1;
     return SWE_OK;
 }
 
-int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, const double* lam_hu,
-                     const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar) {
-    int rc = ready(c);
-    if (rc) return rc;
-    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
-    if (c->params[0].solver != SWE_SOLVER_FWAVE)
-        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave solver");
-    if (!lam_h || !lam_hu || !lam_hv || !out_h || !out_hu || !out_hv || !bbar)
-        return set_error(SWE_E_INVALID, "null cotangent buffer");
-    cudaSetDevice(c->device);
-    GlobalScalars g;
-    CUDA_TRY(cudaMemcpyAsync(&g, c->gs, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
-    const long long t = g.step, k = t - g.dt_seq_base;
-    if (!c->dt_seq || k < 0 || k >= c->dt_seq_len)
-        return set_error(SWE_E_STATE, "the adjoint needs a frozen dt sequence covering step %lld", t);
-    if (!branch) {
-        // forward step t -> t+1 recording the branches; x_t stays in buffer t & 1
-        if (!c->branch && (rc = device_alloc((void**)&c->branch, (size_t)c->cells_total))) return rc;
-        if ((rc = launch_steps(c, 1, c->branch))) return rc;
-        branch = c->branch;
-    }
+}  // extern "C"
+
+namespace {
+// The reverse of step t (the context's state is x_t, parity t & 1).
+int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double* lam_h, const double* lam_hu,
+                   const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar) {
+    const long long k = t - c->seq_base_mirror;
     AdjointArgs A;
     const int in = (int)(t & 1);
     A.h = c->h[in];
@@ -994,8 +1018,7 @@ int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, con
     A.tasks = reinterpret_cast<const int4*>(c->tasks);
     A.seg_ptr = c->seg_ptr;
     A.seg_info = reinterpret_cast<const int4*>(c->seg_info);
-    CUDA_TRY(cudaMemcpyAsync(&A.P, c->ip, sizeof(InstParams), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    A.P = c->ip_host[0];
     A.dt = c->dt_seq_host[(size_t)k];
     A.n_seg = (int32_t)c->n_seg;
     A.seg_cells = c->seg_cells;
@@ -1006,14 +1029,42 @@ int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, con
     // 256 threads per CTA so an SM still has two CTAs' worth of warps
     const int threads = 256;
     const size_t smem = (size_t)21 * c->seg_cells * sizeof(double);
-    CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, threads, smem));
-    if (per_sm < 1) return set_error(SWE_E_INVALID, "adjoint tiling does not fit an SM");
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * c->num_sms, c->n_seg));
-    adjoint_kernel<<<grid, threads, smem, c->stream>>>(A);
+    if (c->adj_seg_cells != c->seg_cells) {
+        CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, threads, smem));
+        if (per_sm < 1) return set_error(SWE_E_INVALID, "adjoint tiling does not fit an SM");
+        c->adj_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * c->num_sms, c->n_seg));
+        c->adj_seg_cells = c->seg_cells;
+    }
+    adjoint_kernel<<<c->adj_grid, threads, smem, c->stream>>>(A);
     CUDA_TRY(cudaGetLastError());
     return SWE_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, const double* lam_hu,
+                     const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
+    if (c->params[0].solver != SWE_SOLVER_FWAVE)
+        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave solver");
+    if (!lam_h || !lam_hu || !lam_hv || !out_h || !out_hu || !out_hv || !bbar)
+        return set_error(SWE_E_INVALID, "null cotangent buffer");
+    cudaSetDevice(c->device);
+    const long long t = c->step_mirror, k = t - c->seq_base_mirror;
+    if (!c->dt_seq || k < 0 || k >= c->dt_seq_len)
+        return set_error(SWE_E_STATE, "the adjoint needs a frozen dt sequence covering step %lld", t);
+    if (!branch) {
+        // forward step t -> t+1 recording the branches; x_t stays in buffer t & 1
+        if (!c->branch && (rc = device_alloc((void**)&c->branch, (size_t)c->cells_total))) return rc;
+        if ((rc = launch_steps(c, 1, c->branch))) return rc;  // the context moves to step t + 1
+        branch = c->branch;
+    }
+    return launch_adjoint(c, t, branch, lam_h, lam_hu, lam_hv, out_h, out_hu, out_hv, bbar);
 }
 
 int swe_ensemble_get_refinements(swe_ctx* c, int8_t* flags, int64_t* n_refinements) {
@@ -1131,6 +1182,218 @@ int swe_mesh_uniform(int32_t depth, int64_t* n_cells, int64_t* n_edges, int64_t*
                      int8_t* bnd_local, double* centroids) {
     return mesh_uniform(depth, n_cells, n_edges, n_bnd, depth_out, plotter_out, edge_cells, edge_local, bnd_cell,
                         bnd_local, centroids);
+}
+
+}  // extern "C"
+
+namespace {
+
+// min(C(n, k), cap + 1), exactly (every partial product C(n - k + i, i) is an integer)
+int64_t binom_capped(int64_t n, int64_t k, int64_t cap) {
+    if (k < 0 || k > n) return 0;
+    k = std::min(k, n - k);
+    unsigned __int128 v = 1;
+    for (int64_t i = 1; i <= k; ++i) {
+        v = v * (unsigned __int128)(n - k + i) / (unsigned __int128)i;
+        if (v > (unsigned __int128)cap) return cap + 1;
+    }
+    return (int64_t)v;
+}
+
+// First checkpoint offset for reversing `length` steps with the start state held
+// and `free` more slots (revolve's offline rule, the same as adjoint.py's
+// binomial_split): with c = free + 1 checkpoints and r repetitions C(c + r, c)
+// steps can be reversed; the tail gets what c - 1 checkpoints reverse with r.
+int64_t binomial_split(int64_t length, int64_t free_slots) {
+    if (length <= 1 || free_slots <= 0) return 1;
+    const int64_t c = free_slots + 1;
+    int64_t r = 0;
+    while (binom_capped(c + r, c, length) < length) ++r;
+    const int64_t tail = binom_capped(c - 1 + r, c - 1, length);
+    return std::max<int64_t>(1, length - std::min<int64_t>(tail, length - 1));
+}
+
+struct Sweep {
+    swe_ctx* c = nullptr;
+    long long s0 = 0;          // the context's step at the start (sweep step t is device step s0 + t)
+    int64_t T = 0, N = 0, stride = 0, G = 0;
+    double* slots = nullptr;   // [slot][3][N]
+    std::vector<int> free_slots;
+    uint8_t* branches = nullptr;  // [T][stride]
+    const int64_t* gauges = nullptr;
+    const double* obs = nullptr;  // [T][G]
+    double* gv = nullptr;         // [T][G]
+    std::vector<char> done;
+    double* lam[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    int li = 0;
+    double* bbar = nullptr;
+    int64_t cur = 0;
+    int64_t forward_steps = 0, adjoint_steps = 0;
+    int rc = SWE_OK;
+
+    double* slot(int k, int q) { return slots + ((size_t)k * 3 + (size_t)q) * (size_t)N; }
+
+    int store(int64_t t, int* out) {
+        if (free_slots.empty()) return set_error(SWE_E_STATE, "revolve ran out of snapshot slots");
+        const int k = free_slots.back();
+        free_slots.pop_back();
+        const int b = (int)((s0 + t) & 1);
+        const size_t bytes = (size_t)N * 8;
+        CUDA_TRY(cudaMemcpyAsync(slot(k, 0), c->h[b], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(slot(k, 1), c->hu[b], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(slot(k, 2), c->hv[b], bytes, cudaMemcpyDeviceToDevice, c->stream));
+        *out = k;
+        return SWE_OK;
+    }
+    int restore(int k, int64_t t) {
+        const int b = (int)((s0 + t) & 1);
+        const size_t bytes = (size_t)N * 8;
+        CUDA_TRY(cudaMemcpyAsync(c->h[b], slot(k, 0), bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(c->hu[b], slot(k, 1), bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(c->hv[b], slot(k, 2), bytes, cudaMemcpyDeviceToDevice, c->stream));
+        set_step_kernel<<<1, 1, 0, c->stream>>>(c->gs, s0 + t);
+        CUDA_TRY(cudaGetLastError());
+        c->step_mirror = s0 + t;
+        cur = t;
+        return SWE_OK;
+    }
+    int advance(int64_t k) {
+        for (int64_t i = 0; i < k; ++i) {
+            const int64_t t = cur;
+            int r = launch_steps(c, 1, branches + (size_t)t * (size_t)stride);
+            if (r) return r;
+            if (!done[(size_t)t]) {  // the first visit of step t records the gauges of x_{t+1}
+                gauge_kernel<<<(int)std::min<int64_t>((G + 127) / 128, 1024), 128, 0, c->stream>>>(
+                    c->gs, c->h[0], c->h[1], G, gauges, N, gv + (size_t)t * (size_t)G);
+                CUDA_TRY(cudaGetLastError());
+                done[(size_t)t] = 1;
+            }
+            cur = t + 1;
+            ++forward_steps;
+        }
+        return SWE_OK;
+    }
+    int adjoint(int64_t t) {
+        if (cur != t) return set_error(SWE_E_STATE, "revolve: state at %lld, reverse step %lld", (long long)cur,
+                                       (long long)t);
+        if (!done[(size_t)t]) {  // run step t once (branches, gauges), then x_t is still in its buffer
+            int r = advance(1);
+            if (r) return r;
+            set_step_kernel<<<1, 1, 0, c->stream>>>(c->gs, s0 + t);
+            CUDA_TRY(cudaGetLastError());
+            c->step_mirror = s0 + t;
+            cur = t;
+        }
+        double** in = lam[li];
+        double** out = lam[li ^ 1];
+        gauge_residual_kernel<<<1, 32, 0, c->stream>>>(in[0], gauges, G, gv + (size_t)t * (size_t)G,
+                                                       obs + (size_t)t * (size_t)G);
+        CUDA_TRY(cudaGetLastError());
+        int r = launch_adjoint(c, s0 + t, branches + (size_t)t * (size_t)stride, in[0], in[1], in[2], out[0],
+                               out[1], out[2], bbar);
+        if (r) return r;
+        li ^= 1;
+        ++adjoint_steps;
+        return SWE_OK;
+    }
+    int rev(int64_t a, int64_t b, int64_t sl, int slot_a) {
+        const int64_t length = b - a;
+        int r;
+        if (length == 1) {
+            if ((r = restore(slot_a, a))) return r;
+            return adjoint(a);
+        }
+        if (sl == 0) {
+            for (int64_t t = b - 1; t >= a; --t) {
+                if ((r = restore(slot_a, a)) || (r = advance(t - a)) || (r = adjoint(t))) return r;
+            }
+            return SWE_OK;
+        }
+        const int64_t m = a + binomial_split(length, sl);
+        int slot_m = -1;
+        if ((r = restore(slot_a, a)) || (r = advance(m - a)) || (r = store(m, &slot_m))) return r;
+        if ((r = rev(m, b, sl - 1, slot_m))) return r;
+        free_slots.push_back(slot_m);
+        return rev(a, m, sl, slot_a);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int swe_gauge_gradient(swe_ctx* c, int64_t n_steps, const double* dts, int32_t snapshots, int64_t n_gauges,
+                       const int64_t* gauges, const double* obs, double* gauge_values, double* grad_h,
+                       double* grad_hu, double* grad_hv, double* grad_b, double* J, int64_t* forward_steps) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
+    if (c->params[0].solver != SWE_SOLVER_FWAVE)
+        return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave solver");
+    if (n_steps < 1 || !dts || snapshots < 1 || n_gauges < 1 || !gauges || !obs || !grad_h || !grad_b || !J)
+        return set_error(SWE_E_INVALID, "bad arguments");
+    cudaSetDevice(c->device);
+    Sweep S;
+    S.c = c;
+    S.T = n_steps;
+    S.N = c->mesh[0].n_cells;
+    S.stride = c->cells_total;
+    S.G = n_gauges;
+    S.gauges = gauges;
+    S.obs = obs;
+    {  // gauge cells must be cells of the mesh
+        std::vector<int64_t> g((size_t)n_gauges);
+        CUDA_TRY(cudaMemcpy(g.data(), gauges, sizeof(int64_t) * g.size(), cudaMemcpyDeviceToHost));
+        for (int64_t v : g)
+            if (v < 0 || v >= S.N) return set_error(SWE_E_INVALID, "gauge cell %lld out of range", (long long)v);
+    }
+    if ((rc = swe_set_dt_sequence(c, n_steps, dts))) return rc;
+    S.s0 = c->step_mirror;
+    const size_t nb = (size_t)S.N * 8;
+    double* work = nullptr;  // lam[2][3], out gauge values if not given
+    const size_t n_work = 6 * (size_t)S.N + (gauge_values ? 0 : (size_t)n_steps * (size_t)n_gauges) + 1;
+    if ((rc = device_alloc((void**)&work, n_work * 8))) return rc;
+    if ((rc = device_alloc((void**)&S.slots, (size_t)snapshots * 3 * nb))) {
+        cudaFree(work);
+        return rc;
+    }
+    if ((rc = device_alloc((void**)&S.branches, (size_t)n_steps * (size_t)S.stride))) {
+        cudaFree(work);
+        cudaFree(S.slots);
+        return rc;
+    }
+    for (int i = 0; i < 2; ++i)
+        for (int q = 0; q < 3; ++q) S.lam[i][q] = work + (size_t)(3 * i + q) * (size_t)S.N;
+    double* dJ = work + 6 * (size_t)S.N;
+    S.gv = gauge_values ? gauge_values : dJ + 1;
+    S.bbar = grad_b;
+    S.done.assign((size_t)n_steps, 0);
+    for (int k = snapshots - 1; k >= 0; --k) S.free_slots.push_back(k);
+    cudaError_t e = cudaMemsetAsync(S.lam[0][0], 0, 3 * nb, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(grad_b, 0, nb, c->stream);
+    if (e != cudaSuccess) rc = set_error(SWE_E_CUDA, "gauge gradient: %s", cudaGetErrorString(e));
+    int slot0 = -1;
+    S.cur = 0;
+    if (!rc) rc = S.store(0, &slot0);
+    if (!rc) rc = S.rev(0, n_steps, snapshots - 1, slot0);
+    if (!rc) rc = S.restore(slot0, 0);  // leave the context at x_0, step s0
+    if (!rc) {
+        misfit_kernel<<<1, 256, 0, c->stream>>>(S.gv, obs, n_steps * n_gauges, dJ);
+        e = cudaGetLastError();
+        double* out[3] = {grad_h, grad_hu, grad_hv};
+        for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+            if (out[q]) e = cudaMemcpyAsync(out[q], S.lam[S.li][q], nb, cudaMemcpyDeviceToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(J, dJ, 8, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) rc = set_error(SWE_E_CUDA, "gauge gradient: %s", cudaGetErrorString(e));
+    }
+    cudaStreamSynchronize(c->stream);
+    cudaFree(work);
+    cudaFree(S.slots);
+    cudaFree(S.branches);
+    if (forward_steps) *forward_steps = S.forward_steps;
+    if (!rc) rc = check_device_error(c);
+    return rc;
 }
 
 }  // extern "C"
