@@ -154,6 +154,12 @@ int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
 int swe_set_arith(swe_ctx* ctx, int32_t mode);
 int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads);
 
+/* Vertices of the cells of swe_mesh_uniform(depth) in the unit square, in the
+ * same cell order: vertices[6 k + 2 v + {0, 1}] = (x, y) of vertex v of cell k
+ * (exact dyadic values). The node coordinates samoa_get_grid hands out
+ * (src/Generic/samoa.h:25-57), per cell; used by the headless VTK writer. */
+int swe_mesh_uniform_vertices(int32_t depth, double* vertices);
+
 /* Uniform Sierpinski mesh of the unit square at reference depth `depth`
  * (2^(depth+1) cells) in traversal order, restating init_grid
  * (src/SFC_node_traversal.f90:22-145). Call with NULL outputs to get the sizes.
@@ -226,6 +232,11 @@ int swe_step_back(swe_ctx* ctx);
  * context is left at step t+1, else it stays at step t. */
 int swe_adjoint_step(swe_ctx* ctx, const uint8_t* branch, const double* lam_h, const double* lam_hu,
                      const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar);
+
+/* n_steps steps, each followed by the gauge sample of swe_sample_gauges into
+ * out[step * n_gauges + g] (device): the forward operator of the gauge misfit,
+ * with no host round trip between steps. No counterpart in the reference. */
+int swe_traverse_gauges(swe_ctx* ctx, int64_t n_steps, int64_t n_gauges, const int64_t* cells, double* out);
 
 /* Gradient of the gauge misfit J = sum_t sum_g (h_{t+1}[gauges[g]] - obs[t][g])^2
  * over n_steps f-wave steps with the frozen dt sequence dts (host, n_steps),

@@ -156,9 +156,7 @@ class GaugeProblem:
         L = self.ctx.L
         with torch.cuda.stream(self.stream):
             gv = torch.empty((self.T, len(self.gauges)), dtype=torch.float64, device=self.dev)
-            for t in range(self.T):
-                self.ctx.traverse(1)
-                _lib.check(L.swe_sample_gauges(self.ctx.ptr, len(self.gauges), _vp(self.gauges), _vp(gv[t])))
+            _lib.check(L.swe_traverse_gauges(self.ctx.ptr, self.T, len(self.gauges), _vp(self.gauges), _vp(gv)))
             J = float(((gv - self.obs) ** 2).sum().item())
         self.stats["forward_steps"] += self.T
         if record:

@@ -74,7 +74,7 @@ int set_error(int code, const char* fmt, ...);
 
 int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
                  int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell,
-                 int8_t* bnd_local, double* centroids);
+                 int8_t* bnd_local, double* centroids, double* vertices = nullptr);
 int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
                 const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
                 const int8_t* bnd_local);

@@ -69,7 +69,7 @@ int64_t uniform_boundary_edges(int depth) { return (int64_t)4 << (depth / 2); }
 
 int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
                  int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell, int8_t* bnd_local,
-                 double* centroids) {
+                 double* centroids, double* vertices) {
     if (depth < 0 || depth > 29) return set_error(SWE_E_INVALID, "mesh depth %d out of range 0..29", depth);
     const int64_t n = (int64_t)2 << depth;
     const int64_t nb = uniform_boundary_edges(depth);
@@ -123,6 +123,11 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
             centroids[2 * k] = ((it.x[0][0] + it.x[1][0]) + it.x[2][0]) / 3.0;
             centroids[2 * k + 1] = ((it.x[0][1] + it.x[1][1]) + it.x[2][1]) / 3.0;
         }
+        if (vertices)
+            for (int v = 0; v < 3; ++v) {
+                vertices[6 * k + 2 * v] = it.x[v][0];
+                vertices[6 * k + 2 * v + 1] = it.x[v][1];
+            }
         const int8_t ip = kPrevIdx[c.turtle], ic = kColorIdx[c.turtle], in = kNextIdx[c.turtle];
         // previous crossed edge: the open crossed edge of the previous cell, or the boundary
         if (!c.prev_bnd) {

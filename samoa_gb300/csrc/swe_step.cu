@@ -970,6 +970,22 @@ int swe_sample_gauges(swe_ctx* c, int64_t n_gauges, const int64_t* cells, double
     return SWE_OK;
 }
 
+int swe_traverse_gauges(swe_ctx* c, int64_t n_steps, int64_t n_gauges, const int64_t* cells, double* out) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "gauges are for single-instance contexts");
+    if (n_steps < 0 || n_gauges < 1 || !cells || !out) return set_error(SWE_E_INVALID, "bad gauge arrays");
+    cudaSetDevice(c->device);
+    const int blocks = (int)std::min<int64_t>((n_gauges + 127) / 128, 1024);
+    for (int64_t s = 0; s < n_steps; ++s) {
+        if ((rc = launch_steps(c, 1))) return rc;
+        gauge_kernel<<<blocks, 128, 0, c->stream>>>(c->gs, c->h[0], c->h[1], n_gauges, cells, c->mesh[0].n_cells,
+                                                    out + (size_t)s * (size_t)n_gauges);
+        CUDA_TRY(cudaGetLastError());
+    }
+    return SWE_OK;
+}
+
 int swe_traverse_branches(swe_ctx* c, int64_t n_steps, uint8_t* branch, int64_t stride) {
     int rc = ready(c);
     if (rc) return rc;
@@ -1175,6 +1191,17 @@ int swe_division_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t*
     if (e != cudaSuccess) return set_error(SWE_E_CUDA, "division check: %s", cudaGetErrorString(e));
     *mismatches = (int64_t)got;
     return SWE_OK;
+}
+
+int swe_mesh_uniform_vertices(int32_t depth, double* vertices) {
+    if (!vertices) return set_error(SWE_E_INVALID, "null vertex array");
+    int64_t n = 0, ne = 0, nb = 0;
+    int rc = mesh_uniform(depth, &n, &ne, &nb, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    std::vector<int8_t> d((size_t)n), p((size_t)n), el((size_t)(2 * ne)), bl((size_t)nb);
+    std::vector<int64_t> ec((size_t)(2 * ne)), bc((size_t)nb);
+    return mesh_uniform(depth, &n, &ne, &nb, d.data(), p.data(), ec.data(), el.data(), bc.data(), bl.data(), nullptr,
+                        vertices);
 }
 
 int swe_mesh_uniform(int32_t depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,

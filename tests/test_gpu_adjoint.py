@@ -201,3 +201,31 @@ def test_native_sweep_matches_python_sweep(swe_lib):
         assert abs(J1 - J2) <= 1e-13 * abs(J2)
     finally:
         P.close()
+
+
+def test_traverse_gauges_matches_step_by_step(swe_lib):
+    import torch
+    scn = scenarios.radial_dam_break(log2_cells=12, boundary="slip")
+    g = scn.grid
+    cells = torch.tensor([0, 17, 1000, g.mesh.n_cells - 1], dtype=torch.int64, device="cuda")
+    dt0 = swe.initial_dt(g.mesh, g.h, g.hu, g.hv, g.b, scn.cfg.courant_number)
+    out = []
+    for batched in (True, False):
+        ctx = swe.SweContext(0)
+        try:
+            ctx.set_params(scn.cfg.params())
+            ctx.upload_mesh(g.mesh)
+            ctx.upload_state(g.h, g.hu, g.hv, g.b)
+            ctx.set_time(0.0, dt0)
+            v = torch.empty((7, 4), dtype=torch.float64, device="cuda")
+            if batched:
+                _lib.check(ctx.L.swe_traverse_gauges(ctx.ptr, 7, 4, _vp(cells), _vp(v)))
+            else:
+                for k in range(7):
+                    ctx.traverse(1)
+                    _lib.check(ctx.L.swe_sample_gauges(ctx.ptr, 4, _vp(cells), _vp(v[k])))
+            ctx.synchronize()
+            out.append(v.cpu())
+        finally:
+            ctx.close()
+    assert torch.equal(out[0], out[1])
