@@ -160,6 +160,32 @@ int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads)
  * (src/Generic/samoa.h:25-57), per cell; used by the headless VTK writer. */
 int swe_mesh_uniform_vertices(int32_t depth, double* vertices);
 
+/* Mesh of the unit square from its leaf depths: the cells of a conforming
+ * Sierpinski tree in traversal order given by their depths (depth[k] of cell
+ * k); the same walk as swe_mesh_uniform (init_grid with the tree's own
+ * bisections) gives the plotter types, the edge streams in the swe_mesh_upload
+ * layout, and optionally centroids[2n] and vertices[6n]. With plotter_out and
+ * the edge arrays NULL only the counts *n_edges, *n_bnd are returned (sizes:
+ * edge_cells, edge_local 2 * n_edges; bnd_cell, bnd_local n_bnd).
+ * SWE_E_INVALID if the depths are not the leaves of such a tree or the tree is
+ * not conforming. The host side of the remesh handoff. */
+int swe_mesh_build(int64_t n_cells, const int8_t* depth, int64_t* n_edges, int64_t* n_bnd, int8_t* plotter_out,
+                   int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell, int8_t* bnd_local, double* centroids,
+                   double* vertices);
+
+/* One remesh from the step's refinement flags (-1 coarsen, 0 keep, 1 refine):
+ * the adaption traversal's conformity closure and refine/coarsen rules
+ * (src/Conformity/Conformity.f90:1244-1317, src/SWE/SWE_adapt.f90:95-169).
+ * Input: the mesh as leaf depths in traversal order, the flags, and optionally
+ * the state h, hu, hv, b (host arrays, n_cells). Output: *n_out cells; with
+ * depth_out non-NULL (capacity >= *n_out) the new leaf depths and, for each
+ * given input, the transferred state (refined cells copy their parent's values,
+ * merged siblings average them, order 0). Call once with depth_out = NULL for
+ * the count. The new mesh's streams come from swe_mesh_build. */
+int swe_mesh_adapt(int64_t n_cells, const int8_t* depth, const int8_t* flags, const double* h, const double* hu,
+                   const double* hv, const double* b, int64_t capacity, int64_t* n_out, int8_t* depth_out,
+                   double* h_out, double* hu_out, double* hv_out, double* b_out);
+
 /* Uniform Sierpinski mesh of the unit square at reference depth `depth`
  * (2^(depth+1) cells) in traversal order, restating init_grid
  * (src/SFC_node_traversal.f90:22-145). Call with NULL outputs to get the sizes.

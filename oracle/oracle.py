@@ -41,6 +41,8 @@ def lib():
         L.oracle_normal.argtypes = [i32, i32, P]
         L.oracle_mesh_uniform.restype = i64
         L.oracle_mesh_uniform.argtypes = [i32, P, P]
+        L.oracle_mesh_from_depths.restype = i64
+        L.oracle_mesh_from_depths.argtypes = [i64, P, P, P]
         L.oracle_mesh_edges.restype = i32
         L.oracle_mesh_edges.argtypes = [P, i64, P, P, P, P, P, P]
         L.oracle_geoclaw_solver.argtypes = [i32] + [dbl] * 10 + [P, P, P]
@@ -86,6 +88,21 @@ def mesh_uniform(depth):
     coords = np.zeros((n, 3, 2), np.float64)
     got = lib().oracle_mesh_uniform(depth, _p(cells5), _p(coords))
     assert got == n
+    m = dict(n=n, cells5=cells5, coords=coords)
+    m.update(mesh_edges(cells5))
+    return m
+
+
+def mesh_from_depths(depths):
+    """Mesh of the tree whose leaves in traversal order have these depths (an
+    adaptive conforming mesh); same outputs as mesh_uniform."""
+    d = np.ascontiguousarray(depths, np.int8)
+    n = len(d)
+    cells5 = np.zeros((n, 5), np.int8)
+    coords = np.zeros((n, 3, 2), np.float64)
+    got = lib().oracle_mesh_from_depths(n, _p(d), _p(cells5), _p(coords))
+    if got != n:
+        raise RuntimeError("oracle_mesh_from_depths failed: %d" % got)
     m = dict(n=n, cells5=cells5, coords=coords)
     m.update(mesh_edges(cells5))
     return m

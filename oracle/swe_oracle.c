@@ -300,6 +300,65 @@ int64_t oracle_mesh_uniform(int depth, int8_t* cells_out, double* coords_out)
     return n;
 }
 
+/* The same recursion over a tree given by its leaf depths in traversal order
+ * (an adaptive conforming mesh): a cell is bisected while it is shallower than
+ * the next leaf's depth. */
+static int sfc_recursion_depths(or_mesh_builder* mb, const or_cell* cell, const double* co, const int8_t* depths)
+{
+    if (mb->n >= mb->cap) return -1;
+    const int target = depths[mb->n];
+    if (cell->depth == target) {
+        mb->cells[mb->n] = *cell;
+        memcpy(mb->coords + 6 * mb->n, co, 6 * sizeof(double));
+        mb->n++;
+        return 0;
+    }
+    if (cell->depth > target || target > OR_MAX_DEPTH) return -2;
+    or_cell a, b;
+    create_child_cells(cell, &a, &b);
+    double mid[2] = { 0.5 * (co[0] + co[4]), 0.5 * (co[1] + co[5]) };
+    double ca[6] = { co[0], co[1], mid[0], mid[1], co[2], co[3] };
+    double cb[6] = { co[2], co[3], mid[0], mid[1], co[4], co[5] };
+    int rc = sfc_recursion_depths(mb, &a, ca, depths);
+    if (rc) return rc;
+    return sfc_recursion_depths(mb, &b, cb, depths);
+}
+
+/*
+ * Mesh of the tree whose n leaves, in traversal order, have the given depths
+ * (init_section + the recursion of sfc_init_recursion applied to that tree).
+ * Outputs as oracle_mesh_uniform. Returns n, or < 0 if the depths are not the
+ * leaves of such a tree.
+ */
+int64_t oracle_mesh_from_depths(int64_t n, const int8_t* depths, int8_t* cells_out, double* coords_out)
+{
+    or_mesh_builder mb;
+    mb.cells = (or_cell*)malloc(sizeof(or_cell) * (size_t)n);
+    mb.coords = (double*)malloc(sizeof(double) * 6 * (size_t)n);
+    mb.n = 0;
+    mb.cap = n;
+    or_cell first = { 8 + 2 + E_OLD, 0, -2, T_K, C_RED };      /* FIRST_OLD_BND */
+    or_cell second = { 4 + 2 + E_NEW, 0, -6, T_H, C_RED };     /* LAST_NEW_BND */
+    const double c1[6] = { 0.0, 0.0, 1.0, 0.0, 1.0, 1.0 };
+    const double c2[6] = { 1.0, 1.0, 0.0, 1.0, 0.0, 0.0 };
+    int rc = sfc_recursion_depths(&mb, &first, c1, depths);
+    if (!rc) rc = sfc_recursion_depths(&mb, &second, c2, depths);
+    if (!rc && mb.n != n) rc = -3;
+    if (!rc) {
+        for (int64_t i = 0; i < n; ++i) {
+            cells_out[5 * i + 0] = mb.cells[i].entity;
+            cells_out[5 * i + 1] = mb.cells[i].depth;
+            cells_out[5 * i + 2] = mb.cells[i].plotter;
+            cells_out[5 * i + 3] = mb.cells[i].turtle;
+            cells_out[5 * i + 4] = mb.cells[i].color;
+        }
+        if (coords_out) memcpy(coords_out, mb.coords, sizeof(double) * 6 * (size_t)n);
+    }
+    free(mb.cells);
+    free(mb.coords);
+    return rc ? rc : n;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Static traversal: which edge a cell's local edge index refers to            */
 /* ------------------------------------------------------------------------- */

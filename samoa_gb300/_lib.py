@@ -23,7 +23,7 @@ EXPORTS = [
     "swe_traverse_graph", "swe_set_dt_sequence", "swe_step_noalloc", "swe_snapshot_store", "swe_snapshot_restore",
     "swe_sample_gauges", "swe_adjoint_step", "swe_set_arith", "swe_traverse_branches", "swe_step_back",
     "swe_division_check", "swe_step_host", "swe_gauge_gradient",
-    "swe_traverse_gauges", "swe_mesh_uniform_vertices",
+    "swe_traverse_gauges", "swe_mesh_uniform_vertices", "swe_mesh_build", "swe_mesh_adapt",
 ]
 
 
@@ -93,6 +93,8 @@ def load():
         "swe_gauge_gradient": [P, i64, P, i32, i64, P, P, P, P, P, P, P, P, P],
         "swe_traverse_gauges": [P, i64, i64, P, P],
         "swe_mesh_uniform_vertices": [i32, P],
+        "swe_mesh_build": [i64, P, P, P, P, P, P, P, P, P, P],
+        "swe_mesh_adapt": [i64, P, P, P, P, P, P, i64, P, P, P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

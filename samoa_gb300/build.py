@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libsamoa_swe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-O2,-fno-fast-math",
               "-Xcompiler", "-ffp-contract=off"]
-SOURCES = ["swe_step.cu", "swe_mesh.cpp", "swe_geometry.cpp", "swe_noalloc.cu", "swe_step_fma.cu"]
+SOURCES = ["swe_step.cu", "swe_mesh.cpp", "swe_geometry.cpp", "swe_noalloc.cu", "swe_step_fma.cu", "swe_adapt.cpp"]
 # the FMA-contraction variant of the step kernels (an opt-in arithmetic mode)
 FLAGS_OVERRIDE = {"swe_step_fma.cu": ["--fmad=true"]}
 

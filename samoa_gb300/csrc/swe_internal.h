@@ -3,6 +3,7 @@
 
 #include <stdint.h>
 
+#include <utility>
 #include <vector>
 
 #include "../../include/samoa_swe.h"
@@ -72,6 +73,31 @@ struct HostMesh {
 
 int set_error(int code, const char* fmt, ...);
 
+// A mesh built by the Sierpinski walk from its leaf depths (swe_mesh.cpp).
+struct BuiltMesh {
+    int64_t n = 0, ne = 0, nb = 0;
+    std::vector<int8_t> depth, plotter, el, bl;
+    std::vector<int64_t> ec, bc;
+    std::vector<double> vert;     // 6 per cell (optional)
+    std::vector<int64_t> parent;  // the bisected node a leaf came from (negative for the two roots)
+};
+// Result of one remesh (swe_adapt.cpp): new leaf depths in traversal order, for
+// each new cell its source cell(s) (second = -1 unless two siblings merged),
+// and the transferred h, hu, hv, b (empty where no input was given).
+struct AdaptResult {
+    int64_t n = 0;
+    std::vector<int8_t> depth;
+    std::vector<std::pair<int64_t, int64_t>> source;
+    std::vector<double> state[4];
+    void reserve_hint(int64_t n0) {
+        depth.reserve((size_t)n0 + (size_t)n0 / 4);
+        source.reserve((size_t)n0 + (size_t)n0 / 4);
+    }
+};
+int mesh_adapt(int64_t n, const int8_t* depth, const int8_t* flags, const double* const in[4], AdaptResult& out);
+int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, bool want_vertices, BuiltMesh& m);
+int export_mesh(const BuiltMesh& m, int8_t* depth_out, int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local,
+                int64_t* bnd_cell, int8_t* bnd_local, double* centroids, double* vertices);
 int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
                  int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell,
                  int8_t* bnd_local, double* centroids, double* vertices = nullptr);

@@ -67,6 +67,131 @@ const int8_t kNextIdx[4] = {0, 2, 1, 1};
 
 int64_t uniform_boundary_edges(int depth) { return (int64_t)4 << (depth / 2); }
 
+// The Sierpinski walk of init_grid over a tree given by its leaf depths in
+// traversal order (depth-first bisection with an explicit stack: a node is
+// bisected while it is shallower than the next leaf's depth), numbering the
+// edges the way the traversal's colour-edge stacks meet them. A uniform mesh
+// is the sequence of 2^(d+1) leaves of depth d.
+int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, bool want_vertices, BuiltMesh& m) {
+    const bool uniform = leaf_depth == nullptr;
+    if (uniform) n_leaves = (int64_t)2 << uniform_depth;
+    if (n_leaves < 2) return set_error(SWE_E_INVALID, "a mesh has at least the two root cells");
+    m.n = n_leaves;
+    m.depth.assign((size_t)n_leaves, 0);
+    m.plotter.assign((size_t)n_leaves, 0);
+    m.parent.assign((size_t)n_leaves, 0);
+    m.ec.assign((size_t)(3 * n_leaves), -1);  // at most (3 n) / 2 edges, two cells each
+    m.el.assign((size_t)(3 * n_leaves), 0);
+    m.bc.clear();
+    m.bl.clear();
+    if (want_vertices) m.vert.assign((size_t)(6 * n_leaves), 0.0);
+    else m.vert.clear();
+
+    struct Item {
+        GrammarCell c;
+        double x[3][2];
+        int64_t parent;
+    };
+    std::vector<Item> stack;
+    stack.reserve(2 * (size_t)kMaxDepth + 8);
+    // the two root triangles of the unit square (init_section, src/SFC_node_traversal.f90:90-109);
+    // pushed in reverse so the first one is expanded first
+    Item r2{{0, 1, 3, 0, -6, kH, kRed}, {{1, 1}, {0, 1}, {0, 0}}, -2};
+    Item r1{{1, 0, 2, 0, -2, kK, kRed}, {{0, 0}, {1, 0}, {1, 1}}, -1};
+    stack.push_back(r2);
+    stack.push_back(r1);
+
+    std::vector<int64_t> color_stack[2];
+    int64_t open_crossed = -1, next_edge = 0, k = 0, node = 0;
+    while (!stack.empty()) {
+        Item it = stack.back();
+        stack.pop_back();
+        if (k >= n_leaves) return set_error(SWE_E_INVALID, "depth sequence ends before the tree does");
+        const int target = uniform ? uniform_depth : leaf_depth[k];
+        if (target < 0 || target > kMaxDepth)
+            return set_error(SWE_E_INVALID, "cell %lld: depth %d out of range", (long long)k, target);
+        if (it.c.depth < target) {
+            Item a, b;
+            bisect(it.c, a.c, b.c);
+            double mx = 0.5 * (it.x[0][0] + it.x[2][0]), my = 0.5 * (it.x[0][1] + it.x[2][1]);
+            a.x[0][0] = it.x[0][0]; a.x[0][1] = it.x[0][1];
+            a.x[1][0] = mx; a.x[1][1] = my;
+            a.x[2][0] = it.x[1][0]; a.x[2][1] = it.x[1][1];
+            b.x[0][0] = it.x[1][0]; b.x[0][1] = it.x[1][1];
+            b.x[1][0] = mx; b.x[1][1] = my;
+            b.x[2][0] = it.x[2][0]; b.x[2][1] = it.x[2][1];
+            a.parent = b.parent = node++;
+            stack.push_back(b);
+            stack.push_back(a);
+            continue;
+        }
+        if (it.c.depth > target)
+            return set_error(SWE_E_INVALID, "cell %lld: depth %d is not a leaf of the tree (node depth %d)",
+                             (long long)k, target, it.c.depth);
+        // a leaf: cell number k in traversal order
+        const GrammarCell& c = it.c;
+        m.depth[(size_t)k] = c.depth;
+        m.plotter[(size_t)k] = c.plotter;
+        m.parent[(size_t)k] = it.parent;
+        if (want_vertices)
+            for (int v = 0; v < 3; ++v) {
+                m.vert[(size_t)(6 * k + 2 * v)] = it.x[v][0];
+                m.vert[(size_t)(6 * k + 2 * v + 1)] = it.x[v][1];
+            }
+        const int8_t ip = kPrevIdx[c.turtle], ic = kColorIdx[c.turtle], in = kNextIdx[c.turtle];
+        // previous crossed edge: the open crossed edge of the previous cell, or the boundary
+        if (!c.prev_bnd) {
+            if (open_crossed < 0) return set_error(SWE_E_INVALID, "mesh walk: missing crossed edge");
+            m.ec[(size_t)(2 * open_crossed + 1)] = k;
+            m.el[(size_t)(2 * open_crossed + 1)] = ip;
+        } else {
+            m.bc.push_back(k);
+            m.bl.push_back(ip);
+        }
+        open_crossed = -1;
+        // colour edge: first touch pushes, second touch pops
+        std::vector<int64_t>& cs = color_stack[c.color + 1];
+        if (c.color_type == 0) {
+            if (cs.empty()) return set_error(SWE_E_INVALID, "mesh walk: colour stack underflow (not conforming)");
+            int64_t e = cs.back();
+            cs.pop_back();
+            m.ec[(size_t)(2 * e + 1)] = k;
+            m.el[(size_t)(2 * e + 1)] = ic;
+        } else if (c.color_type == 1) {
+            int64_t e = next_edge++;
+            cs.push_back(e);
+            m.ec[(size_t)(2 * e)] = k;
+            m.el[(size_t)(2 * e)] = ic;
+        } else {
+            m.bc.push_back(k);
+            m.bl.push_back(ic);
+        }
+        // next crossed edge
+        if (!c.next_bnd) {
+            int64_t e = next_edge++;
+            m.ec[(size_t)(2 * e)] = k;
+            m.el[(size_t)(2 * e)] = in;
+            open_crossed = e;
+        } else {
+            m.bc.push_back(k);
+            m.bl.push_back(in);
+        }
+        ++k;
+    }
+    if (k != n_leaves) return set_error(SWE_E_INVALID, "depth sequence longer than the tree");
+    if (open_crossed >= 0 || !color_stack[0].empty() || !color_stack[1].empty())
+        return set_error(SWE_E_INVALID, "mesh walk inconsistent (not conforming)");
+    m.ne = next_edge;
+    m.nb = (int64_t)m.bc.size();
+    if (2 * m.ne + m.nb != 3 * m.n) return set_error(SWE_E_INVALID, "mesh walk: edge count inconsistent");
+    for (int64_t e = 0; e < m.ne; ++e)
+        if (m.ec[(size_t)(2 * e + 1)] < 0) return set_error(SWE_E_INVALID, "mesh walk: edge %lld has one cell",
+                                                            (long long)e);
+    m.ec.resize((size_t)(2 * m.ne));
+    m.el.resize((size_t)(2 * m.ne));
+    return SWE_OK;
+}
+
 int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,
                  int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local, int64_t* bnd_cell, int8_t* bnd_local,
                  double* centroids, double* vertices) {
@@ -77,100 +202,32 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
     if (n_cells) *n_cells = n;
     if (n_edges) *n_edges = ne;
     if (n_bnd) *n_bnd = nb;
-    if (!depth_out && !plotter_out && !edge_cells && !edge_local && !bnd_cell && !bnd_local && !centroids)
+    if (!depth_out && !plotter_out && !edge_cells && !edge_local && !bnd_cell && !bnd_local && !centroids &&
+        !vertices)
         return SWE_OK;
     if (!depth_out || !plotter_out || !edge_cells || !edge_local || !bnd_cell || !bnd_local)
         return set_error(SWE_E_INVALID, "mesh outputs must all be given (centroids optional)");
+    BuiltMesh m;
+    int rc = build_mesh(n, nullptr, depth, centroids || vertices, m);
+    if (rc) return rc;
+    return export_mesh(m, depth_out, plotter_out, edge_cells, edge_local, bnd_cell, bnd_local, centroids, vertices);
+}
 
-    // Depth-first bisection with an explicit stack; leaves come out in curve order.
-    struct Item {
-        GrammarCell c;
-        double x[3][2];
-    };
-    std::vector<Item> stack;
-    stack.reserve(2 * (size_t)depth + 8);
-    // the two root triangles of the unit square (init_section, src/SFC_node_traversal.f90:90-109);
-    // pushed in reverse so the first one is expanded first
-    Item r2{{0, 1, 3, 0, -6, kH, kRed}, {{1, 1}, {0, 1}, {0, 0}}};
-    Item r1{{1, 0, 2, 0, -2, kK, kRed}, {{0, 0}, {1, 0}, {1, 1}}};
-    stack.push_back(r2);
-    stack.push_back(r1);
-
-    std::vector<int64_t> color_stack[2];
-    int64_t open_crossed = -1, next_edge = 0, next_bnd = 0, k = 0;
-    while (!stack.empty()) {
-        Item it = stack.back();
-        stack.pop_back();
-        if (it.c.depth < depth) {
-            Item a, b;
-            bisect(it.c, a.c, b.c);
-            double mx = 0.5 * (it.x[0][0] + it.x[2][0]), my = 0.5 * (it.x[0][1] + it.x[2][1]);
-            a.x[0][0] = it.x[0][0]; a.x[0][1] = it.x[0][1];
-            a.x[1][0] = mx; a.x[1][1] = my;
-            a.x[2][0] = it.x[1][0]; a.x[2][1] = it.x[1][1];
-            b.x[0][0] = it.x[1][0]; b.x[0][1] = it.x[1][1];
-            b.x[1][0] = mx; b.x[1][1] = my;
-            b.x[2][0] = it.x[2][0]; b.x[2][1] = it.x[2][1];
-            stack.push_back(b);
-            stack.push_back(a);
-            continue;
+int export_mesh(const BuiltMesh& m, int8_t* depth_out, int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local,
+                int64_t* bnd_cell, int8_t* bnd_local, double* centroids, double* vertices) {
+    if (depth_out) std::memcpy(depth_out, m.depth.data(), (size_t)m.n);
+    if (plotter_out) std::memcpy(plotter_out, m.plotter.data(), (size_t)m.n);
+    if (edge_cells) std::memcpy(edge_cells, m.ec.data(), sizeof(int64_t) * 2 * (size_t)m.ne);
+    if (edge_local) std::memcpy(edge_local, m.el.data(), 2 * (size_t)m.ne);
+    if (bnd_cell) std::memcpy(bnd_cell, m.bc.data(), sizeof(int64_t) * (size_t)m.nb);
+    if (bnd_local) std::memcpy(bnd_local, m.bl.data(), (size_t)m.nb);
+    if (centroids && !m.vert.empty())
+        for (int64_t k = 0; k < m.n; ++k) {
+            const double* x = &m.vert[(size_t)(6 * k)];
+            centroids[2 * k] = ((x[0] + x[2]) + x[4]) / 3.0;
+            centroids[2 * k + 1] = ((x[1] + x[3]) + x[5]) / 3.0;
         }
-        // a leaf: cell number k in traversal order
-        const GrammarCell& c = it.c;
-        depth_out[k] = c.depth;
-        plotter_out[k] = c.plotter;
-        if (centroids) {
-            centroids[2 * k] = ((it.x[0][0] + it.x[1][0]) + it.x[2][0]) / 3.0;
-            centroids[2 * k + 1] = ((it.x[0][1] + it.x[1][1]) + it.x[2][1]) / 3.0;
-        }
-        if (vertices)
-            for (int v = 0; v < 3; ++v) {
-                vertices[6 * k + 2 * v] = it.x[v][0];
-                vertices[6 * k + 2 * v + 1] = it.x[v][1];
-            }
-        const int8_t ip = kPrevIdx[c.turtle], ic = kColorIdx[c.turtle], in = kNextIdx[c.turtle];
-        // previous crossed edge: the open crossed edge of the previous cell, or the boundary
-        if (!c.prev_bnd) {
-            if (open_crossed < 0) return set_error(SWE_E_INVALID, "mesh walk: missing crossed edge");
-            edge_cells[2 * open_crossed + 1] = k;
-            edge_local[2 * open_crossed + 1] = ip;
-        } else {
-            bnd_cell[next_bnd] = k;
-            bnd_local[next_bnd++] = ip;
-        }
-        open_crossed = -1;
-        // colour edge: first touch pushes, second touch pops
-        std::vector<int64_t>& cs = color_stack[c.color + 1];
-        if (c.color_type == 0) {
-            if (cs.empty()) return set_error(SWE_E_INVALID, "mesh walk: colour stack underflow");
-            int64_t e = cs.back();
-            cs.pop_back();
-            edge_cells[2 * e + 1] = k;
-            edge_local[2 * e + 1] = ic;
-        } else if (c.color_type == 1) {
-            int64_t e = next_edge++;
-            cs.push_back(e);
-            edge_cells[2 * e] = k;
-            edge_local[2 * e] = ic;
-        } else {
-            bnd_cell[next_bnd] = k;
-            bnd_local[next_bnd++] = ic;
-        }
-        // next crossed edge
-        if (!c.next_bnd) {
-            int64_t e = next_edge++;
-            edge_cells[2 * e] = k;
-            edge_local[2 * e] = in;
-            open_crossed = e;
-        } else {
-            bnd_cell[next_bnd] = k;
-            bnd_local[next_bnd++] = in;
-        }
-        ++k;
-    }
-    if (k != n || next_edge != ne || next_bnd != nb || open_crossed >= 0 || !color_stack[0].empty() ||
-        !color_stack[1].empty())
-        return set_error(SWE_E_INVALID, "mesh walk inconsistent");
+    if (vertices && !m.vert.empty()) std::memcpy(vertices, m.vert.data(), sizeof(double) * 6 * (size_t)m.n);
     return SWE_OK;
 }
 

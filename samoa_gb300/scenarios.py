@@ -49,6 +49,42 @@ def radial_dam_break(log2_cells=16, boundary="slip", solver="fwave", mesh=None):
     return Scenario("radial_dam_break", _grid(mesh, cfg, h, b), cfg, 100)
 
 
+def apriori_mesh(cfg, surface, max_cells=1 << 26):
+    """The a-priori refinement loop of the SWE initialisation (src/SWE/SWE.f90:232-269
+    with the criteria of src/SWE/SWE_initialize.f90:292-322): starting from the two
+    root cells, refine every cell shallower than the minimum depth, and every
+    cell shallower than the maximum depth whose initial surface differs between
+    its three vertices (the probes at barycentric (1,0), (0,0), (0,1)); remesh
+    with conformity; repeat until no cell asks for refinement. `surface(x, y)`
+    gives the initial surface at world points."""
+    from .swe import adapt, mesh_from_depths
+    mesh = mesh_from_depths(np.zeros(2, np.int8), vertices=True)
+    while True:
+        v = cfg.scaling * mesh.vertices + np.asarray(cfg.offset, np.float64)
+        s = surface(v[:, :, 0], v[:, :, 1])
+        d = mesh.depth
+        want = (d < cfg.i_min_depth) | ((d < cfg.i_max_depth) & (s.max(axis=1) > s.min(axis=1)))
+        if not want.any():
+            return mesh
+        mesh, _ = adapt(mesh, want.astype(np.int8))
+        if mesh.n_cells > max_cells:
+            raise ValueError("a-priori refinement exceeds %d cells" % max_cells)
+
+
+def adaptive_dam_break(min_depth=6, max_depth=12, solver="fwave", boundary="outflow"):
+    """The reference's default SWE initial state (src/SWE/SWE_initialize.f90:349-370):
+    surface 1 m for x < 0 and 0 m elsewhere, at rest, over a flat bottom at -10 m,
+    on the mesh of the a-priori refinement (max depth along the step, min depth
+    elsewhere); dt from the initial CFL estimate."""
+    cfg = Config(flux_solver=solver, boundary=boundary, courant_number=0.45, dry_tolerance=0.01, scaling=1.0,
+                 offset=(-0.5, -0.5), i_min_depth=min_depth, i_max_depth=max_depth)
+    surface = lambda x, y: np.where(x < 0.0, 1.0, 0.0)
+    mesh = apriori_mesh(cfg, surface)
+    x, y = _world(mesh, cfg)
+    b = np.full(mesh.n_cells, -10.0)
+    return Scenario("adaptive_dam_break", _grid(mesh, cfg, surface(x, y), b), cfg, 50)
+
+
 def bowl_bathymetry(x, y, h0=10.0, a=0.4):
     r2 = x * x + y * y
     return -h0 * (1.0 - r2 / (a * a))

@@ -59,6 +59,7 @@ class Mesh:
     bnd_local: np.ndarray      # int8[nb]
     centroids: np.ndarray = None  # float64[n, 2] in the unit square (optional)
     version: int = 0
+    vertices: np.ndarray = None   # float64[n, 3, 2] in the unit square (optional)
 
     @property
     def n_cells(self):
@@ -80,6 +81,43 @@ def uniform_mesh(depth, centroids=True):
     cen = np.empty((n, 2), np.float64) if centroids else None
     _lib.check(L.swe_mesh_uniform(depth, None, None, None, _p(d), _p(p), _p(ec), _p(el), _p(bc), _p(bl), _p(cen)))
     return Mesh(d, p, ec, el, bc, bl, cen)
+
+
+def mesh_from_depths(depths, centroids=True, vertices=False):
+    """Mesh of the conforming Sierpinski tree whose leaves, in traversal order,
+    have the given depths (swe_mesh_build)."""
+    L = _lib.load()
+    d = np.ascontiguousarray(depths, np.int8)
+    n = len(d)
+    ne, nb = C.c_int64(), C.c_int64()
+    _lib.check(L.swe_mesh_build(n, _p(d), C.byref(ne), C.byref(nb), *([None] * 7)))
+    ne, nb = ne.value, nb.value
+    p = np.empty(n, np.int8)
+    ec = np.empty((ne, 2), np.int64)
+    el = np.empty((ne, 2), np.int8)
+    bc = np.empty(nb, np.int64)
+    bl = np.empty(nb, np.int8)
+    cen = np.empty((n, 2), np.float64) if centroids else None
+    ver = np.empty((n, 3, 2), np.float64) if vertices else None
+    _lib.check(L.swe_mesh_build(n, _p(d), None, None, _p(p), _p(ec), _p(el), _p(bc), _p(bl), _p(cen), _p(ver)))
+    return Mesh(d.copy(), p, ec, el, bc, bl, cen, vertices=ver)
+
+
+def adapt(mesh, flags, h=None, hu=None, hv=None, b=None):
+    """One remesh from refinement flags (-1, 0, 1; the step's output): returns the
+    new mesh and the transferred (h, hu, hv, b) (None where not given)."""
+    L = _lib.load()
+    f = np.ascontiguousarray(flags, np.int8)
+    ins = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (h, hu, hv, b)]
+    n_out = C.c_int64()
+    _lib.check(L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], 0, C.byref(n_out),
+                                None, None, None, None, None))
+    m = n_out.value
+    d = np.empty(m, np.int8)
+    outs = [None if a is None else np.empty(m, np.float64) for a in ins]
+    _lib.check(L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], m, C.byref(n_out),
+                                _p(d), *[_p(a) for a in outs]))
+    return mesh_from_depths(d, centroids=mesh.centroids is not None, vertices=mesh.vertices is not None), outs
 
 
 @dataclass
