@@ -43,6 +43,10 @@ def parse():
     ap.add_argument("--solver", default="fwave")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-tune", action="store_true", help="skip the tiling autotuner (default tiling)")
+    ap.add_argument("--no-adaptive", action="store_true")
+    ap.add_argument("--adaptive-min-depth", type=int, default=12)
+    ap.add_argument("--adaptive-max-depth", type=int, default=18)
+    ap.add_argument("--adaptive-steps", type=int, default=20)
     ap.add_argument("--tune-log2-cells", type=int, default=22)
     ap.add_argument("--cpu-sample-log2", type=int, default=22)
     ap.add_argument("--cpu-steps", type=int, default=8)
@@ -280,6 +284,27 @@ def ensemble_compare(a, device):
                     "per instance on one stream"}
 
 
+def adaptive_compare(a, device):
+    """The adaptive wet/dry bowl (augmented Riemann, dry tolerance 1e-3) with a
+    host remesh before every step (nadapt 1): device time of the steps against
+    host time of the remeshes (swe_mesh_adapt + swe_mesh_build + upload)."""
+    from samoa_gb300 import scenarios, swe
+    t0 = time.perf_counter()
+    scn = scenarios.adaptive_bowl(min_depth=a.adaptive_min_depth, max_depth=a.adaptive_max_depth)
+    t_init = time.perf_counter() - t0
+    g = scn.grid
+    (mesh, *_), st = swe.run_adaptive(scn.cfg, g.mesh, g.h, g.hu, g.hv, g.b, g.r_dt, a.adaptive_steps,
+                                      adapt_every=1, bathymetry=scenarios.bowl_bathymetry, device=device)
+    return {"workload": "adaptive_bowl_aug_riemann_dmin%d_dmax%d" % (a.adaptive_min_depth, a.adaptive_max_depth),
+            "steps": st["steps"], "cells_first": st["cells"][0], "cells_last": st["cells"][-1],
+            "apriori_refinement_s": t_init, "step_cell_updates_per_s": st["cell_updates"] / st["step_s"],
+            "remesh_s_per_step": st["remesh_s"] / max(1, st["remeshes"]),
+            "step_s_per_step": st["step_s"] / st["steps"],
+            "end_to_end_cell_updates_per_s": st["cell_updates"] / (st["step_s"] + st["remesh_s"]),
+            "note": "remesh before every step from the previous step's flags (host C++: conformity, "
+                    "refine/coarsen, order-0 transfer, edge streams), then upload; the step itself on the GPU"}
+
+
 def adjoint_compare(a, device):
     """Gauge-misfit gradient through the adjoint against the forward run it
     differentiates: 2^18 cells, 2,000 steps, 64 snapshots, f-wave, frozen dt;
@@ -476,6 +501,12 @@ def run_gpu(a, rank, world, local):
                 ensemble = ensemble_compare(a, local)
             except Exception as exc:  # reported, never hides the headline number
                 ensemble = {"error": repr(exc)[:300]}
+        adaptive = None
+        if world == 1 and not a.no_adaptive:
+            try:
+                adaptive = adaptive_compare(a, local)
+            except Exception as exc:
+                adaptive = {"error": repr(exc)[:300]}
         adj = None
         if world == 1 and not a.no_adjoint:
             try:
@@ -498,6 +529,7 @@ def run_gpu(a, rank, world, local):
             "e2e": e2e,
             "ensemble": ensemble,
             "adjoint": adj,
+            "adaptive": adaptive,
             "gpu_launches": a.steps,
             "clocks": clk,
             "sim": {"time": sim_time, "dt": dt},

@@ -178,13 +178,15 @@ int swe_mesh_build(int64_t n_cells, const int8_t* depth, int64_t* n_edges, int64
  * (src/Conformity/Conformity.f90:1244-1317, src/SWE/SWE_adapt.f90:95-169).
  * Input: the mesh as leaf depths in traversal order, the flags, and optionally
  * the state h, hu, hv, b (host arrays, n_cells). Output: *n_out cells; with
- * depth_out non-NULL (capacity >= *n_out) the new leaf depths and, for each
- * given input, the transferred state (refined cells copy their parent's values,
+ * depth_out non-NULL (capacity >= *n_out) the new leaf depths, optionally the
+ * source cell of each new cell (source_out: the parent of a refined cell, the
+ * first of two merged siblings; compare depths to tell which), and for each
+ * given input the transferred state (refined cells copy their parent's values,
  * merged siblings average them, order 0). Call once with depth_out = NULL for
  * the count. The new mesh's streams come from swe_mesh_build. */
 int swe_mesh_adapt(int64_t n_cells, const int8_t* depth, const int8_t* flags, const double* h, const double* hu,
                    const double* hv, const double* b, int64_t capacity, int64_t* n_out, int8_t* depth_out,
-                   double* h_out, double* hu_out, double* hv_out, double* b_out);
+                   int64_t* source_out, double* h_out, double* hu_out, double* hv_out, double* b_out);
 
 /* Uniform Sierpinski mesh of the unit square at reference depth `depth`
  * (2^(depth+1) cells) in traversal order, restating init_grid

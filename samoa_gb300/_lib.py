@@ -94,7 +94,7 @@ def load():
         "swe_traverse_gauges": [P, i64, i64, P, P],
         "swe_mesh_uniform_vertices": [i32, P],
         "swe_mesh_build": [i64, P, P, P, P, P, P, P, P, P, P],
-        "swe_mesh_adapt": [i64, P, P, P, P, P, P, i64, P, P, P, P, P, P],
+        "swe_mesh_adapt": [i64, P, P, P, P, P, P, i64, P, P, P, P, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -162,7 +162,7 @@ int swe_mesh_build(int64_t n_cells, const int8_t* depth, int64_t* n_edges, int64
 
 int swe_mesh_adapt(int64_t n_cells, const int8_t* depth, const int8_t* flags, const double* h, const double* hu,
                    const double* hv, const double* b, int64_t capacity, int64_t* n_out, int8_t* depth_out,
-                   double* h_out, double* hu_out, double* hv_out, double* b_out) {
+                   int64_t* source_out, double* h_out, double* hu_out, double* hv_out, double* b_out) {
     using namespace swe;
     if (!n_out) return set_error(SWE_E_INVALID, "null n_out");
     const double* in[4] = {h, hu, hv, b};
@@ -178,6 +178,8 @@ int swe_mesh_adapt(int64_t n_cells, const int8_t* depth, const int8_t* flags, co
         return set_error(SWE_E_INVALID, "adapt: %lld cells do not fit capacity %lld", (long long)r.n,
                          (long long)capacity);
     std::memcpy(depth_out, r.depth.data(), (size_t)r.n);
+    if (source_out)
+        for (int64_t i = 0; i < r.n; ++i) source_out[i] = r.source[(size_t)i].first;
     for (int q = 0; q < 4; ++q)
         if (outp[q]) std::memcpy(outp[q], r.state[q].data(), sizeof(double) * (size_t)r.n);
     return SWE_OK;

@@ -110,6 +110,26 @@ def parabolic_bowl(log2_cells=14, seed=2, solver="aug_riemann", amplitude=0.5, s
     return Scenario("parabolic_bowl", _grid(mesh, cfg, h, b), cfg, 500)
 
 
+def adaptive_bowl(min_depth=12, max_depth=22, seed=2, solver="aug_riemann", amplitude=0.5, sigma=0.05):
+    """The parabolic bowl on the mesh of the a-priori refinement between the given
+    depths (the adaptive wet/dry configuration: the Gaussian surface differs
+    between the vertices of every cell, so the initial mesh is uniform at the
+    maximum depth; the flags of the step then coarsen the flat water)."""
+    cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=1e-3, scaling=1.0,
+                 offset=(-0.5, -0.5), i_min_depth=min_depth, i_max_depth=max_depth)
+    rng = np.random.default_rng(seed)
+    x0, y0 = rng.uniform(-0.1, 0.1, 2)
+    eta_f = lambda x, y: amplitude * np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / (2 * sigma * sigma))
+    mesh = apriori_mesh(cfg, eta_f)
+    x, y = _world(mesh, cfg)
+    b = bowl_bathymetry(x, y)
+    eta = eta_f(x, y)
+    h = np.where(b < eta, eta, b)
+    scn = Scenario("adaptive_bowl", _grid(mesh, cfg, h, b), cfg, 500)
+    scn.bathymetry = bowl_bathymetry
+    return scn
+
+
 def value_noise(x, y, seed, octaves=5, base=8.0, persistence=0.5):
     """Seeded lattice value noise in [-1, 1], smooth-step interpolated, summed over
     octaves (frequency doubling, amplitude times ``persistence``). x, y in [-0.5, 0.5]."""

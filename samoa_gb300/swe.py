@@ -103,21 +103,24 @@ def mesh_from_depths(depths, centroids=True, vertices=False):
     return Mesh(d.copy(), p, ec, el, bc, bl, cen, vertices=ver)
 
 
-def adapt(mesh, flags, h=None, hu=None, hv=None, b=None):
+def adapt(mesh, flags, h=None, hu=None, hv=None, b=None, with_source=False):
     """One remesh from refinement flags (-1, 0, 1; the step's output): returns the
-    new mesh and the transferred (h, hu, hv, b) (None where not given)."""
+    new mesh and the transferred (h, hu, hv, b) (None where not given), and with
+    with_source also each new cell's source cell."""
     L = _lib.load()
     f = np.ascontiguousarray(flags, np.int8)
     ins = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (h, hu, hv, b)]
     n_out = C.c_int64()
     _lib.check(L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], 0, C.byref(n_out),
-                                None, None, None, None, None))
+                                None, None, None, None, None, None))
     m = n_out.value
     d = np.empty(m, np.int8)
+    src = np.empty(m, np.int64)
     outs = [None if a is None else np.empty(m, np.float64) for a in ins]
     _lib.check(L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], m, C.byref(n_out),
-                                _p(d), *[_p(a) for a in outs]))
-    return mesh_from_depths(d, centroids=mesh.centroids is not None, vertices=mesh.vertices is not None), outs
+                                _p(d), _p(src), *[_p(a) for a in outs]))
+    new = mesh_from_depths(d, centroids=mesh.centroids is not None, vertices=mesh.vertices is not None)
+    return (new, outs, src) if with_source else (new, outs)
 
 
 @dataclass
@@ -383,3 +386,59 @@ def initial_dt(mesh: Mesh, h, hu, hv, b, courant):
         if smax > 0.0:
             best = min(best, vols[dd] / (edges * smax))
     return courant * best
+
+
+def run_adaptive(cfg, mesh, h, hu, hv, b, dt, steps, adapt_every=1, bathymetry=None, device=0, time=0.0):
+    """The SWE run loop with host remeshing (src/SWE/SWE.f90:378-392): step i
+    (from 1) is preceded by a remesh when i % adapt_every == 0, from the
+    refinement flags of the step before (swe_mesh_adapt + swe_mesh_build, then
+    an upload); refined cells take b from `bathymetry(x, y)` when it is given
+    (get_bathymetry_at_element of refine_op), else their parent's. Returns the
+    final (mesh, h, hu, hv, b, time, dt) and timings: device seconds of the steps
+    (CUDA events) and host seconds of the remeshes and uploads."""
+    import time as _time
+
+    import torch
+    ctx = SweContext(device)
+    stream = torch.cuda.Stream(device=device)
+    ctx.set_stream(stream.cuda_stream)
+    stats = {"steps": 0, "cell_updates": 0, "step_s": 0.0, "remesh_s": 0.0, "remeshes": 0, "cells": []}
+    try:
+        ctx.set_params(cfg.params())
+        ctx.upload_mesh(mesh)
+        ctx.upload_state(h, hu, hv, b)
+        ctx.set_time(time, dt)
+        flags = np.zeros(mesh.n_cells, np.int8)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for i in range(1, steps + 1):
+            if adapt_every > 0 and i % adapt_every == 0 and i > 1:
+                t0 = _time.perf_counter()
+                h, hu, hv, b = ctx.download_state()
+                time, dt, _ = ctx.get_time()
+                new, (h, hu, hv, b), src = adapt(mesh, flags, h, hu, hv, b, with_source=True)
+                if bathymetry is not None:
+                    fine = new.depth > mesh.depth[src]
+                    if fine.any():
+                        x = cfg.scaling * new.centroids[fine, 0] + cfg.offset[0]
+                        y = cfg.scaling * new.centroids[fine, 1] + cfg.offset[1]
+                        b[fine] = bathymetry(x, y)
+                mesh = new
+                ctx.upload_mesh(mesh)
+                ctx.upload_state(h, hu, hv, b)
+                ctx.set_time(time, dt)
+                stats["remesh_s"] += _time.perf_counter() - t0
+                stats["remeshes"] += 1
+            e0.record(stream)
+            ctx.traverse(1)
+            e1.record(stream)
+            e1.synchronize()
+            stats["step_s"] += e0.elapsed_time(e1) * 1e-3
+            stats["steps"] += 1
+            stats["cell_updates"] += mesh.n_cells
+            stats["cells"].append(mesh.n_cells)
+            flags, _ = ctx.refinements()
+        h, hu, hv, b = ctx.download_state()
+        time, dt, _ = ctx.get_time()
+    finally:
+        ctx.close()
+    return (mesh, h, hu, hv, b, time, dt), stats

@@ -69,8 +69,9 @@ def test_adapt_invariants(swe_lib):
     assert np.array_equal(h0, h)
     # refine everything: every cell is split at least once (the conformity
     # closure splits some twice where a coarser neighbour meets a finer one)
-    m1, (src1, _, _, _) = swe.adapt(mesh, np.ones(n, np.int8), np.arange(n, dtype=np.float64))
-    assert np.all(m1.depth >= mesh.depth[src1.astype(int)] + 1)
+    m1, (src1, _, _, _), s1 = swe.adapt(mesh, np.ones(n, np.int8), np.arange(n, dtype=np.float64), with_source=True)
+    assert np.array_equal(src1.astype(np.int64), s1)
+    assert np.all(m1.depth >= mesh.depth[s1] + 1)
     assert m1.n_cells >= 2 * n
     # on a uniform mesh: refine all, then coarsen all returns to the start bit for bit
     u = swe.uniform_mesh(6)

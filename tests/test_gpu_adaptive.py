@@ -19,7 +19,7 @@ def _upload(ctx, scn, mesh, h, hu, hv, b, time, dt):
     ctx.set_time(time, dt)
 
 
-@pytest.mark.parametrize("solver", ["fwave", "aug_riemann", "llf_bath"])
+@pytest.mark.parametrize("solver", ["fwave", "aug_riemann", "llfbath"])
 def test_adaptive_mesh_step_bitexact(swe_lib, oracle_lib, solver):
     scn = scenarios.adaptive_dam_break(min_depth=6, max_depth=12, solver=solver, boundary="slip")
     g = scn.grid
@@ -49,7 +49,7 @@ def test_remesh_cycles_bitexact(swe_lib, oracle_lib):
     """Five cycles of four steps, each followed by a host remesh from the last
     step's flags; the oracle walks the same trees with the same transferred
     states, and the GPU matches it bit for bit after every step."""
-    scn = scenarios.adaptive_dam_break(min_depth=6, max_depth=12, solver="fwave", boundary="slip")
+    scn = scenarios.adaptive_bowl(min_depth=6, max_depth=11, solver="fwave")
     g = scn.grid
     P = oracle_params(scn.cfg)
     mesh, h, hu, hv, b, t, dt = g.mesh, g.h, g.hu, g.hv, g.b, g.r_time, g.r_dt
@@ -74,3 +74,19 @@ def test_remesh_cycles_bitexact(swe_lib, oracle_lib):
     finally:
         ctx.close()
     assert len(set(sizes)) > 1  # the mesh did change
+
+
+def test_run_adaptive_bowl(swe_lib):
+    """The run loop with a remesh before every step on the wet/dry bowl: the
+    mesh coarsens the flat water, and the water volume changes only through the
+    wet/dry clamps and the re-sampled bathymetry of refined cells."""
+    scn = scenarios.adaptive_bowl(min_depth=6, max_depth=10)
+    g = scn.grid
+    vol0 = np.sum((g.h - g.b) * np.ldexp(1.0, -(g.mesh.depth.astype(int) + 1)))
+    (mesh, h, hu, hv, b, t, dt), st = swe.run_adaptive(scn.cfg, g.mesh, g.h, g.hu, g.hv, g.b, g.r_dt, 8,
+                                                       bathymetry=scenarios.bowl_bathymetry)
+    assert st["steps"] == 8 and st["remeshes"] == 7
+    assert mesh.n_cells < g.mesh.n_cells
+    vol = np.sum((h - b) * np.ldexp(1.0, -(mesh.depth.astype(int) + 1)))
+    assert abs(vol - vol0) < 1e-2 * vol0
+    assert t > 0 and dt > 0
