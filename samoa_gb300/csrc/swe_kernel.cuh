@@ -367,11 +367,13 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             double ds = z0(leg * upd[(3 * 3 + k0) * T + i]) + hyp * upd[(3 * 3 + 1) * T + i];
             ds = ds + leg * upd[(3 * 3 + k2) * T + i];
             int8_t f = 0;
-            const double nrm = fabs(dh);
-            if (d < P.max_depth && lt(P.thr_refine, nrm)) {
+            // |dh| > thr and |dh| < thr / 8 on the bit patterns (thresholds are positive;
+            // a NaN |dh| passes neither test, as in IEEE)
+            const long long nrm = abs_bits(dh);
+            if (d < P.max_depth && not_nan(nrm) && nrm > __double_as_longlong(P.thr_refine)) {
                 f = 1;
                 ++nref;
-            } else if (d > P.min_depth && lt(nrm, P.thr_coarsen)) {
+            } else if (d > P.min_depth && nrm < __double_as_longlong(P.thr_coarsen)) {
                 f = -1;
             }
             if (P.dt_by_max) {  // ds >= 0, so its bits order like its value
