@@ -358,14 +358,14 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
             const int d = A.depth[c];
             const int di = d - P.dmin;
             const double leg = tab_leg[di], hyp = tab_hyp[di], ndv = tab_ndv[di];
-            double dh = z0(leg * upd[(0 * 3 + k0) * T + i]) + hyp * upd[(0 * 3 + 1) * T + i];
-            dh = dh + leg * upd[(0 * 3 + k2) * T + i];
-            double dp1 = z0(leg * upd[(1 * 3 + k0) * T + i]) + hyp * upd[(1 * 3 + 1) * T + i];
-            dp1 = dp1 + leg * upd[(1 * 3 + k2) * T + i];
-            double dp2 = z0(leg * upd[(2 * 3 + k0) * T + i]) + hyp * upd[(2 * 3 + 1) * T + i];
-            dp2 = dp2 + leg * upd[(2 * 3 + k2) * T + i];
-            double ds = z0(leg * upd[(3 * 3 + k0) * T + i]) + hyp * upd[(3 * 3 + 1) * T + i];
-            ds = ds + leg * upd[(3 * 3 + k2) * T + i];
+            double dh = z0(imul_cell(leg, upd[(0 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(0 * 3 + 1) * T + i]);
+            dh = dh + imul_cell(leg, upd[(0 * 3 + k2) * T + i]);
+            double dp1 = z0(imul_cell(leg, upd[(1 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(1 * 3 + 1) * T + i]);
+            dp1 = dp1 + imul_cell(leg, upd[(1 * 3 + k2) * T + i]);
+            double dp2 = z0(imul_cell(leg, upd[(2 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(2 * 3 + 1) * T + i]);
+            dp2 = dp2 + imul_cell(leg, upd[(2 * 3 + k2) * T + i]);
+            double ds = z0(imul_cell(leg, upd[(3 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(3 * 3 + 1) * T + i]);
+            ds = ds + imul_cell(leg, upd[(3 * 3 + k2) * T + i]);
             int8_t f = 0;
             // |dh| > thr and |dh| < thr / 8 on the bit patterns (thresholds are positive;
             // a NaN |dh| passes neither test, as in IEEE)
@@ -377,14 +377,14 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
                 f = -1;
             }
             if (P.dt_by_max) {  // ds >= 0, so its bits order like its value
-                const unsigned long long x = (unsigned long long)__double_as_longlong(ds * tab_pow[di]);
+                const unsigned long long x = (unsigned long long)dbits(imul_cell(ds, tab_pow[di]));
                 dskey = x > dskey ? x : dskey;
             } else {
                 dtmin = dmn(dtmin, tab_vol[di] / ds);
             }
-            dh = ndv * dh;
-            dp1 = ndv * dp1;
-            dp2 = ndv * dp2;
+            dh = imul_cell(ndv, dh);
+            dp1 = imul_cell(ndv, dp1);
+            dp2 = imul_cell(ndv, dp2);
             double h = sh_h[i], p1 = sh_hu[i], p2 = sh_hv[i];
             const double b = sh_b[i];
             uint8_t br = 0;

@@ -14,6 +14,26 @@
 #ifndef SWE_KNS
 #define SWE_KNS swe
 #endif
+// Which products run on the integer pipe (imul) instead of the FP64 pipe: the
+// solver's (delphi, Roe velocity, f-wave coefficients, quotients), the edge
+// rotations' and the cell update's. Off by default: measured on GB300 (2^26-cell
+// basin, autotuned tiling) the step ran at 2.40e9 cell-updates/s with all
+// products on the FP64 pipe, 2.35e9 with the cell update's on the integer pipe,
+// 2.24e9 with the rotations' or the solver's, 1.99e9 with all of them: the
+// integer multiply's ~30-instruction dependency chains stall the 12-16 warps
+// an SM holds at this register count more than the FP64 pipe's queue does.
+#ifndef SWE_IMUL
+#define SWE_IMUL 0
+#endif
+#ifndef SWE_IMUL_SOLVER
+#define SWE_IMUL_SOLVER SWE_IMUL
+#endif
+#ifndef SWE_IMUL_ROT
+#define SWE_IMUL_ROT SWE_IMUL
+#endif
+#ifndef SWE_IMUL_CELL
+#define SWE_IMUL_CELL SWE_IMUL
+#endif
 namespace swe {}
 
 #include <stdint.h>
@@ -33,31 +53,86 @@ struct Update {
     double h, p1, p2, s;  // net update (or flux) and maximum wave speed
 };
 
-__device__ __forceinline__ double z0(double x) {
-    long long v = __double_as_longlong(x);
-    return __longlong_as_double(v == (long long)0x8000000000000000ULL ? 0LL : v);
+// Bit casts the compiler cannot see through: tests on the bit pattern of a double
+// stay integer instructions (with the plain casts the compiler may turn a test
+// such as "bits << 1 == 0" back into an FP64 comparison, on the FP64 pipe).
+__device__ __forceinline__ long long dbits(double x) {
+    long long r;
+    asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+    return r;
 }
+__device__ __forceinline__ double bitsd(long long v) {
+    double r;
+    asm("mov.b64 %0, %1;" : "=d"(r) : "l"(v));
+    return r;
+}
+
+__device__ __forceinline__ double z0(double x) {
+    long long v = dbits(x);
+    return bitsd(v == (long long)0x8000000000000000ULL ? 0LL : v);
+}
+// RN(a * b) on the integer pipe. GB300 retires ~500 G FP64 instructions/s but
+// has a wide integer pipe that the step barely uses; this moves a product
+// there (see SWE_IMUL for what that measured). Normal (or zero) operands with a normal
+// result: the 53 x 53-bit significand product (128-bit, __umul64hi + low half),
+// normalised by at most one bit, rounded to nearest even from the guard bit and
+// a sticky OR of the bits below, exponent ea + eb - bias (+1 on a carry out of
+// the rounding). Subnormal, infinite and NaN operands and results out of the
+// normal range take the FP64 multiply, so every input gives the IEEE product
+// (compared with the FP64 multiply bit for bit on the device by
+// swe_division_check's companion test, swe_multiply_check).
+__device__ __forceinline__ double imul_int(double a, double b) {
+    const unsigned long long A = dbits(a), B = dbits(b);
+    const unsigned long long S = (A ^ B) & 0x8000000000000000ULL;
+    const int ea = (int)((A >> 52) & 0x7ff), eb = (int)((B >> 52) & 0x7ff);
+    const unsigned long long M = 0x000fffffffffffffULL;
+    const bool za = (A << 1) == 0, zb = (B << 1) == 0;
+    if (za || zb) {  // +-0 times a finite number: a signed zero
+        if ((za && eb != 0x7ff) || (zb && ea != 0x7ff)) return bitsd((long long)S);
+        return a * b;
+    }
+    if (ea == 0 || eb == 0 || ea == 0x7ff || eb == 0x7ff) return a * b;
+    const unsigned long long ma = (A & M) | (1ULL << 52), mb = (B & M) | (1ULL << 52);
+    const unsigned long long hi = __umul64hi(ma, mb), lo = ma * mb;
+    const int norm = (int)(hi >> 41) & 1;  // product in [2^105, 2^106)
+    const int sh = 52 + norm;
+    unsigned long long m = (hi << (64 - sh)) | (lo >> sh);
+    const unsigned long long g = (lo >> (sh - 1)) & 1ULL;
+    const bool sticky = (lo & ((1ULL << (sh - 1)) - 1ULL)) != 0;
+    m += (g && (sticky || (m & 1ULL))) ? 1ULL : 0ULL;
+    int e = ea + eb - 1023 + norm;
+    if (m >> 53) {
+        m >>= 1;
+        ++e;
+    }
+    if (e < 1 || e > 2046) return a * b;
+    return bitsd((long long)(S | ((unsigned long long)e << 52) | (m & M)));
+}
+__device__ __forceinline__ double imul(double a, double b) { return SWE_IMUL_SOLVER ? imul_int(a, b) : a * b; }
+__device__ __forceinline__ double imul_rot(double a, double b) { return SWE_IMUL_ROT ? imul_int(a, b) : a * b; }
+__device__ __forceinline__ double imul_cell(double a, double b) { return SWE_IMUL_CELL ? imul_int(a, b) : a * b; }
+
 __device__ __forceinline__ double dmn(double a, double b) { return (a < b) ? a : b; }
 __device__ __forceinline__ double dmx(double a, double b) { return (a > b) ? a : b; }
 
 // IEEE predicates on the integer pipe (bit patterns), exact for every input
 // including +-0, infinities and NaN; the FP64 pipe is the step's bottleneck.
-__device__ __forceinline__ long long abs_bits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+__device__ __forceinline__ long long abs_bits(double x) { return dbits(x) & 0x7fffffffffffffffLL; }
 __device__ __forceinline__ bool not_nan(long long a) { return a <= 0x7ff0000000000000LL; }  // a = abs_bits
 __device__ __forceinline__ bool is_finite(double x) { return abs_bits(x) < 0x7ff0000000000000LL; }
 __device__ __forceinline__ bool lt0(double x) {  // x < 0.0
-    const long long b = __double_as_longlong(x);
+    const long long b = dbits(x);
     const long long a = b & 0x7fffffffffffffffLL;
     return b < 0 && a != 0 && not_nan(a);
 }
 __device__ __forceinline__ bool gt0(double x) {  // x > 0.0
-    const long long b = __double_as_longlong(x);
+    const long long b = dbits(x);
     return b > 0 && b <= 0x7ff0000000000000LL;
 }
 __device__ __forceinline__ bool is_nan(double x) { return abs_bits(x) > 0x7ff0000000000000LL; }
 // A key that orders like the value for non-NaN doubles, with -0 equal to +0.
 __device__ __forceinline__ long long ord_key(double x) {
-    long long b = __double_as_longlong(x);
+    long long b = dbits(x);
     b = (b == (long long)0x8000000000000000ULL) ? 0LL : b;
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
@@ -68,7 +143,7 @@ __device__ __forceinline__ double imin(double a, double b) { return lt(a, b) ? a
 __device__ __forceinline__ double imax(double a, double b) { return lt(b, a) ? a : b; }  // dmx on the integer pipe
 // x with its sign flipped when `neg` (exact, like multiplying by -1)
 __device__ __forceinline__ double flip(double x, bool neg) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+    return bitsd(dbits(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
 }
 
 // ---------------------------------------------------------------------------
@@ -112,12 +187,12 @@ __device__ __forceinline__ double rcp_nr(double b) {
 }
 
 __device__ __forceinline__ bool exp_in(double x, int lo, int hi) {
-    const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+    const int e = (int)((dbits(x) >> 52) & 0x7ff) - 1023;
     return e >= lo && e <= hi;
 }
 
 __device__ __forceinline__ bool recip_fast(double b) {
-    const long long bits = __double_as_longlong(b);
+    const long long bits = dbits(b);
     return exp_in(b, -500, 500) && ((bits & 0x000fffffffffffffLL) != 0x000fffffffffffffLL);
 }
 
@@ -137,9 +212,9 @@ __device__ __forceinline__ Recip recip_rn(double b) {
 
 __device__ __forceinline__ double div_rn(double a, const Recip& r) {
     if (!r.fast) return a / r.b;
-    if ((__double_as_longlong(a) << 1) == 0) return a * r.y;  // +-0 with the IEEE sign
+    if ((dbits(a) << 1) == 0) return a * r.y;  // +-0 with the IEEE sign
     if (!exp_in(a, -500, 500)) return a / r.b;
-    double q = a * r.y;
+    double q = imul(a, r.y);
     double res = fma(-r.b, q, a);
     q = fma(res, r.y, q);
     res = fma(-r.b, q, a);
@@ -334,9 +409,11 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
             bL = hR + bR;
         }
     }
-    double delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) +
-                     (((0.5 * g) * (((bR + hR) - bL) - hL)) * (hR + hL))) -
-                    (((0.5 * g) * (hR + hL)) * (bR - bL));
+    const double hsum = hR + hL;
+    const double ghalf_h = imul(g * 0.5, hsum);  // (0.5 * g) * (hR + hL): delphi, chat, the f-wave's deldelphi
+    double delphi = ((imul(huR - huL, uL + uR) - imul(imul(uL, uR), hR - hL)) +
+                     imul(imul(0.5 * g, ((bR + hR) - bL) - hL), hsum)) -
+                    imul(ghalf_h, bR - bL);
     // sqrt(g * h) after the wet/dry fix-ups: a wet side keeps its depth, a dry one
     // has depth 0, and a wall mirrors the wet side's depth
     // a dry side has h = 0 <= drytol now, a wet one is unchanged, a wall mirrors the wet side
@@ -345,8 +422,8 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     double sqR = wetR ? (wall_r ? sqL0 : sqR0) : 0.0;
     double sL = uL - sqL;
     double sR = uR + sqR;
-    double uhat = div_rn(sqL * uL + sqR * uR, recip_rn(sqR + sqL));
-    double chat = sqrt((g * 0.5) * (hR + hL));
+    double uhat = div_rn(imul(sqL, uL) + imul(sqR, uR), recip_rn(sqR + sqL));
+    double chat = sqrt(ghalf_h);
     double sE1 = imin(sL, uhat - chat);
     double sE2 = imax(sR, uhat + chat);
 
@@ -356,16 +433,16 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     } else {
         double delhu = huR - huL;
         double delb = bR - bL;
-        double deldelphi = -(((g * 0.5) * (hR + hL)) * delb);
+        double deldelphi = -imul(ghalf_h, delb);
         double dpd = delphi - deldelphi;
         const Recip rD = recip_rn(sE2 - sE1);
-        double beta1 = div_rn(sE2 * delhu - dpd, rD);
-        double beta2 = div_rn(dpd - sE1 * delhu, rD);
-        sw[0] = sE1; sw[1] = 0.5 * (sE1 + sE2); sw[2] = sE2;
-        fw[0][0] = beta1; fw[1][0] = beta1 * sE1; fw[2][0] = beta1 * vL;
-        fw[0][2] = beta2; fw[1][2] = beta2 * sE2; fw[2][2] = beta2 * vR;
+        double beta1 = div_rn(imul(sE2, delhu) - dpd, rD);
+        double beta2 = div_rn(dpd - imul(sE1, delhu), rD);
+        sw[0] = sE1; sw[1] = imul(0.5, sE1 + sE2); sw[2] = sE2;
+        fw[0][0] = beta1; fw[1][0] = imul(beta1, sE1); fw[2][0] = imul(beta1, vL);
+        fw[0][2] = beta2; fw[1][2] = imul(beta2, sE2); fw[2][2] = imul(beta2, vR);
         fw[0][1] = 0.0; fw[1][1] = 0.0;
-        fw[2][1] = ((huR * vR - huL * vL) - fw[2][0]) - fw[2][2];
+        fw[2][1] = ((imul(huR, vR) - imul(huL, vL)) - fw[2][0]) - fw[2][2];
     }
     // eliminate ghost fluxes of a wall (multiplication by 0 keeps the sign of zero)
     auto zero_wave = [&](const int w) {
@@ -413,7 +490,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     const long long a1 = abs_bits(sw[1]), a2 = abs_bits(sw[2]);
     if (a1 > m && not_nan(a1)) m = a1;
     if (a2 > m && not_nan(a2)) m = a2;
-    maxspeed = __longlong_as_double(m);
+    maxspeed = bitsd(m);
 }
 
 // compute_geoclaw_flux, src/SWE/SWE_euler_timestep.f90:449-481.
@@ -439,10 +516,10 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         }
     } else {
         // T = [[n1, n2], [-n2, n1]]; p_edge = T p
-        pL1 = z0(n1 * QL.p1) + n2 * QL.p2;
-        pL2 = z0(-n2 * QL.p1) + n1 * QL.p2;
-        pR1 = z0(n1 * QR.p1) + n2 * QR.p2;
-        pR2 = z0(-n2 * QR.p1) + n1 * QR.p2;
+        pL1 = z0(imul_rot(n1, QL.p1)) + imul_rot(n2, QL.p2);
+        pL2 = z0(imul_rot(-n2, QL.p1)) + imul_rot(n1, QL.p2);
+        pR1 = z0(imul_rot(n1, QR.p1)) + imul_rot(n2, QR.p2);
+        pR2 = z0(imul_rot(-n2, QR.p1)) + imul_rot(n1, QR.p2);
     }
     double netL[3], netR[3], ms;
     geoclaw_solver<SOLVER>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, yL, yR, drytol, netL, netR, ms);
@@ -460,10 +537,10 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         }
     } else {
         // p = net(2:3) T
-        fL.p1 = z0(netL[1] * n1) + netL[2] * -n2;
-        fL.p2 = z0(netL[1] * n2) + netL[2] * n1;
-        fR.p1 = z0(netR[1] * n1) + netR[2] * -n2;
-        fR.p2 = z0(netR[1] * n2) + netR[2] * n1;
+        fL.p1 = z0(imul_rot(netL[1], n1)) + imul_rot(netL[2], -n2);
+        fL.p2 = z0(imul_rot(netL[1], n2)) + imul_rot(netL[2], n1);
+        fR.p1 = z0(imul_rot(netR[1], n1)) + imul_rot(netR[2], -n2);
+        fR.p2 = z0(imul_rot(netR[1], n2)) + imul_rot(netR[2], n1);
     }
 }
 
