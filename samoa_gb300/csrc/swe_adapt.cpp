@@ -26,10 +26,12 @@ namespace swe {
 
 namespace {
 
-// Which local edge (0..2) of a cell with plotter type p is its leg (x0, x1),
-// where x0 -> x2 is the hypotenuse and x1 the right-angle vertex of the walk's
-// vertex order: the outward normal of (x0, x1) points along x1 - x2, so its
-// dot product with x2 - x0 is negative, the other leg's positive.
+// Which local edge (0..2) of a cell is its leg (x0, x1), where x0 -> x2 is the
+// hypotenuse and x1 the right-angle vertex of the walk's vertex order: the
+// outward normal of (x0, x1) points along x1 - x2, so its dot product with
+// x2 - x0 is negative, the other leg's positive. (Which end of the hypotenuse
+// comes first is not a function of the plotter type alone, so it is decided
+// per cell from its vertices.)
 struct LegTable {
     double normal[17][3][2];
     LegTable() {
@@ -48,10 +50,10 @@ int leg_a_local(const LegTable& t, int plotter, const double* x) {
 
 int mesh_adapt(int64_t n, const int8_t* depth, const int8_t* flags, const double* const in[4], AdaptResult& out) {
     if (n < 2 || !depth || !flags) return set_error(SWE_E_INVALID, "bad mesh or flags");
+    static const LegTable legs;
     BuiltMesh m;
     int rc = build_mesh(n, depth, 0, true, m);
     if (rc) return rc;
-    static const LegTable legs;
     const int64_t ne = m.ne, nb = m.nb;
     // edge ids: inner edges 0..ne-1, boundary edges ne..ne+nb-1
     std::vector<int64_t> slot((size_t)(3 * n), -1);

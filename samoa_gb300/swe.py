@@ -111,14 +111,20 @@ def adapt(mesh, flags, h=None, hu=None, hv=None, b=None, with_source=False):
     f = np.ascontiguousarray(flags, np.int8)
     ins = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (h, hu, hv, b)]
     n_out = C.c_int64()
-    _lib.check(L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], 0, C.byref(n_out),
-                                None, None, None, None, None, None))
+    cap = 2 * mesh.n_cells + 64  # enough unless most cells refine twice; else a second call with the count
+    for _ in range(2):
+        d = np.empty(cap, np.int8)
+        src = np.empty(cap, np.int64)
+        outs = [None if a is None else np.empty(cap, np.float64) for a in ins]
+        rc = L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], cap, C.byref(n_out),
+                              _p(d), _p(src), *[_p(a) for a in outs])
+        if rc == 0 or n_out.value <= cap:
+            _lib.check(rc)
+            break
+        cap = n_out.value
     m = n_out.value
-    d = np.empty(m, np.int8)
-    src = np.empty(m, np.int64)
-    outs = [None if a is None else np.empty(m, np.float64) for a in ins]
-    _lib.check(L.swe_mesh_adapt(mesh.n_cells, _p(mesh.depth), _p(f), *[_p(a) for a in ins], m, C.byref(n_out),
-                                _p(d), _p(src), *[_p(a) for a in outs]))
+    d, src = d[:m], src[:m]
+    outs = [None if a is None else a[:m] for a in outs]
     new = mesh_from_depths(d, centroids=mesh.centroids is not None, vertices=mesh.vertices is not None)
     return (new, outs, src) if with_source else (new, outs)
 
