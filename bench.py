@@ -191,7 +191,7 @@ def run_reference(a, rank, world):
     sample = "2^%d-cell sample of the basin workload per step (%d cells), %d steps, OpenMP C restatement" % (
         a.cpu_sample_log2, m.n_cells, a.steps)
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": a.steps, "warmup": a.warmup,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1000.0 * t / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "solver": a.solver,

@@ -66,6 +66,15 @@ struct StepArgs {
     int32_t fixed_io;          // 1: read h[0], hu[0], hv[0] and write h[1].. on every step (caller's buffers)
 };
 
+// Launch bounds of the step kernel: at most 256 threads; with SWE_MIN_BLOCKS
+// defined, also that many resident CTAs of 256 threads (registers capped at
+// 65536 / (256 * SWE_MIN_BLOCKS)). Undefined: the compiler's own register choice.
+#ifdef SWE_MIN_BLOCKS
+#define SWE_STEP_BOUNDS __launch_bounds__(256, SWE_MIN_BLOCKS)
+#else
+#define SWE_STEP_BOUNDS __launch_bounds__(256)
+#endif
+
 constexpr int kWaitLimit = 1 << 24;  // polls of an mbarrier before a kernel gives up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -172,7 +181,7 @@ __device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, doub
 }
 
 template <int SOLVER>
-__global__ void __launch_bounds__(256) step_kernel(const StepArgs A) {
+__global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int T = A.seg_cells;
     double* sh_h = reinterpret_cast<double*>(smem_raw);
