@@ -390,9 +390,11 @@ def run_gpu(a, rank, world, local):
                                        device="cuda")
         sg = sample.grid
         best, res = autotune.autotune(sg.mesh, sg.h, sg.hu, sg.hv, sg.b, sample.cfg.params(), sg.r_dt, device=local)
-        ctx.set_tiling(*best)
+        ctx.set_staging(1)
+        ctx.set_tiling(best[0], best[1])
+        ctx.set_staging(best[2])
         tuning = {"sample_cells": sg.mesh.n_cells, "best": list(best),
-                  "ms_per_step": {"%dx%d" % k: round(v * 1e3, 4) for k, v in sorted(res.items())}}
+                  "ms_per_step": {"%dx%d/s%d" % k: round(v * 1e3, 4) for k, v in sorted(res.items())}}
     ctx.upload_mesh(g.mesh)
     ctx.upload_state(g.h, g.hu, g.hv, g.b)
     ctx.set_time(g.r_time, g.r_dt)
@@ -519,7 +521,8 @@ def run_gpu(a, rank, world, local):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "cells": n,
                        "solver": a.solver, "boundary": "outflow", "segment_cells": tiling[0],
-                       "block_threads": tiling[1], "arith": a.arith, "autotune": tuning,
+                       "block_threads": tiling[1], "staging_depth": tuning["best"][2] if tuning else 1,
+                       "arith": a.arith, "autotune": tuning,
                        "l2": "inputs larger than L2 (2.1 GB state)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline,

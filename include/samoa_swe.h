@@ -137,10 +137,18 @@ int swe_synchronize(swe_ctx* ctx);
 int swe_last_error(char* buf, size_t n);
 
 /* Kernel tuning: cells per segment (even, 64..1536; 18 doubles of shared
- * memory per cell) and threads per block (multiple of 32, 64..256); 0 keeps
+ * memory per cell, 22 with staging depth 2, at most 227 KB in all) and threads
+ * per block (multiple of 32, 64..256); 0 keeps
  * the current value. A mesh upload or
  * this call rebuilds the segment task lists. */
 int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
+
+/* Staging depth of the step kernel: 1 = a CTA stages a segment's state into
+ * shared memory, then works on it; 2 = it stages the next segment (bulk copies
+ * in flight) while it works on the current one, at 4 * segment_cells doubles
+ * more shared memory. Default 1; SWE_E_INVALID if the tiling then exceeds
+ * shared memory. No counterpart in the reference. */
+int swe_set_staging(swe_ctx* ctx, int32_t depth);
 
 /* Arithmetic of the step kernel. STRICT (the default): every FP64 operation
  * rounded separately, in the reference's evaluation order, so results are bit

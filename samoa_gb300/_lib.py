@@ -24,7 +24,7 @@ EXPORTS = [
     "swe_sample_gauges", "swe_adjoint_step", "swe_set_arith", "swe_traverse_branches", "swe_step_back",
     "swe_division_check", "swe_step_host", "swe_gauge_gradient",
     "swe_traverse_gauges", "swe_mesh_uniform_vertices", "swe_mesh_build", "swe_mesh_adapt",
-    "swe_multiply_check",
+    "swe_multiply_check", "swe_set_staging",
 ]
 
 
@@ -96,6 +96,7 @@ def load():
         "swe_mesh_uniform_vertices": [i32, P],
         "swe_mesh_build": [i64, P, P, P, P, P, P, P, P, P, P],
         "swe_multiply_check": [i64, C.c_uint64, i32, P],
+        "swe_set_staging": [P, i32],
         "swe_mesh_adapt": [i64, P, P, P, P, P, P, i64, P, P, P, P, P, P, P],
     }
     for name, args in sig.items():

@@ -14,11 +14,13 @@ from . import swe
 
 DEFAULT_SEGMENTS = (256, 384, 448, 512, 640, 768, 1024)
 DEFAULT_THREADS = (128, 256)
+DEFAULT_STAGING = (1, 2)
 
 
 def autotune(mesh, h, hu, hv, b, params, dt, segments=DEFAULT_SEGMENTS, threads=DEFAULT_THREADS, steps=4,
-             device=0):
-    """Return ((segment_cells, block_threads), {tiling: seconds per step}) for the fastest tiling."""
+             device=0, staging=DEFAULT_STAGING):
+    """Return ((segment_cells, block_threads, staging_depth), {setting: seconds per
+    step}) for the fastest setting of segment length, block size and staging depth."""
     import torch
     ctx = swe.SweContext(device)
     results = {}
@@ -27,9 +29,11 @@ def autotune(mesh, h, hu, hv, b, params, dt, segments=DEFAULT_SEGMENTS, threads=
         ctx.upload_mesh(mesh)
         stream = torch.cuda.Stream(device=device)
         ctx.set_stream(stream.cuda_stream)
-        for seg, thr in itertools.product(segments, threads):
+        for depth, seg, thr in itertools.product(staging, segments, threads):
             try:
+                ctx.set_staging(1)
                 ctx.set_tiling(seg, thr)
+                ctx.set_staging(depth)
             except swe._lib.SweError:
                 continue
             ctx.upload_state(h, hu, hv, b)
@@ -42,7 +46,7 @@ def autotune(mesh, h, hu, hv, b, params, dt, segments=DEFAULT_SEGMENTS, threads=
             e1.record(stream)
             e1.synchronize()
             ctx.synchronize()
-            results[(seg, thr)] = e0.elapsed_time(e1) * 1e-3 / steps
+            results[(seg, thr, depth)] = e0.elapsed_time(e1) * 1e-3 / steps
     finally:
         ctx.close()
     best = min(results, key=results.get)

@@ -64,6 +64,7 @@ struct StepArgs {
     int32_t n_seg, n_inst, seg_cells, max_ndepth, n_cells_total;
     int32_t use_tma;
     int32_t fixed_io;          // 1: read h[0], hu[0], hv[0] and write h[1].. on every step (caller's buffers)
+    int32_t stage_depth;       // 1: stage a segment, then work on it; 2: stage the next one meanwhile
 };
 
 // Launch bounds of the step kernel: at most 256 threads; with SWE_MIN_BLOCKS
@@ -184,11 +185,11 @@ template <int SOLVER>
 __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int T = A.seg_cells;
-    double* sh_h = reinterpret_cast<double*>(smem_raw);
-    double* sh_hu = sh_h + T;
-    double* sh_hv = sh_hu + T;
-    double* sh_b = sh_hv + T;
-    double* sh_rh = sh_b + T;       // RN(1 / depth) where the cell is wet
+    // staging buffers [stage_depth][h, hu, hv, b][T]: with depth 2 the next
+    // segment's bulk copies land in one buffer while the CTA works on the other
+    const bool depth2 = A.stage_depth > 1;
+    double* stage = reinterpret_cast<double*>(smem_raw);
+    double* sh_rh = stage + (depth2 ? 8 : 4) * T;  // RN(1 / depth) where the cell is wet
     double* sh_sq = sh_rh + T;      // sqrt(g * depth) where the cell is wet
     double* upd = sh_sq + T;        // [4 quantities][3 local edges][T cells]
     double* tab_leg = upd + 12 * T; // per depth of the current instance
@@ -196,7 +197,7 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     double* tab_vol = tab_hyp + A.max_ndepth;
     double* tab_ndv = tab_vol + A.max_ndepth;  // -dt / volume
     double* tab_pow = tab_ndv + A.max_ndepth;  // 2^(d+1)
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar[2];
     __shared__ double red_min[32];
     __shared__ unsigned long long red_max[32];
     __shared__ long long red_sum[32];
@@ -218,7 +219,8 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
 
     if (tid == 0) {
         s_error = 0;
-        mbar_init(&bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         fence_mbar_init();
     }
     __syncthreads();
@@ -226,17 +228,71 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     double dtmin = DBL_MAX;  // r_dt_new = huge(1.0) (pre_traversal_op, :133-140)
     unsigned long long dskey = 0;  // bits of max ds * 2^(d+1) (dt_by_max)
     long long nref = 0;
-    uint32_t phase = 0;
+    uint32_t phase = 0;    // bit k: parity of barrier k
+    uint32_t pending = 0;  // bit k: bulk copies in flight into buffer k
     int cur = -1;
     InstParams P;
 
+    // Stage segment `sg` into buffer k: bulk copies of the 16-byte multiple (the
+    // segment starts at an even cell) completing on barrier k, plain loads for an
+    // odd tail cell or for host memory. All threads call it.
+    auto issue = [&](int sg, int k) {
+        const int4 si = __ldg(&A.seg_info[sg]);
+        const int c0 = si.x, cn = si.y;
+        double* bh = stage + (size_t)k * 4 * T;
+        const int cbulk = A.use_tma ? (cn & ~1) : 0;
+        if (cbulk > 0) {
+            if (tid == 0) {
+                fence_proxy_async();
+                const uint32_t bytes = (uint32_t)cbulk * 8u;
+                mbar_arrive_expect_tx(&bar[k], 4u * bytes);
+                bulk_g2s(bh, hin + c0, bytes, &bar[k]);
+                bulk_g2s(bh + T, huin + c0, bytes, &bar[k]);
+                bulk_g2s(bh + 2 * T, hvin + c0, bytes, &bar[k]);
+                bulk_g2s(bh + 3 * T, A.b + c0, bytes, &bar[k]);
+            }
+            pending |= 1u << k;
+        }
+        for (int i = cbulk + tid; i < cn; i += blockDim.x) {
+            bh[i] = hin[c0 + i];
+            bh[T + i] = huin[c0 + i];
+            bh[2 * T + i] = hvin[c0 + i];
+            bh[3 * T + i] = A.b[c0 + i];
+        }
+    };
+    // Wait (one thread, bounded) for buffer k's bulk copies.
+    auto wait = [&](int k) {
+        if (pending & (1u << k)) {
+            if (tid == 0) {
+                int polls = 0;
+                while (!mbar_try_wait(&bar[k], (phase >> k) & 1u)) {
+                    if (++polls > kWaitLimit) {
+                        s_error = 2u;
+                        break;
+                    }
+                }
+            }
+            phase ^= 1u << k;
+            pending &= ~(1u << k);
+        }
+    };
+
     // segments are handed out dynamically (CTAs that draw cheap segments, e.g.
     // dry land, take more); each CTA still sees its segments in increasing order
-    for (;;) {
-        if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
-        __syncthreads();
-        const int seg = s_seg;
-        if (seg >= A.n_seg) break;
+    if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+    __syncthreads();
+    int seg = s_seg;
+    int kbuf = 0;
+    if (seg < A.n_seg) issue(seg, 0);
+    while (seg < A.n_seg) {
+        int seg_next = A.n_seg;
+        if (depth2) {  // draw and stage the next segment before working on this one
+            __syncthreads();
+            if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+            __syncthreads();
+            seg_next = s_seg;
+            if (seg_next < A.n_seg) issue(seg_next, kbuf ^ 1);
+        }
         const int4 si = __ldg(&A.seg_info[seg]);
         const int c0 = si.x, cn = si.y, inst = si.z;
         if (inst != cur) {  // uniform across the CTA
@@ -254,37 +310,14 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             }
             cur = inst;
         }
-        // ---- 1. stage the segment's state
-        const int cbulk = A.use_tma ? (cn & ~1) : 0;  // 16-byte multiple (c0 is even)
-        if (cbulk > 0 && tid == 0) {
-            fence_proxy_async();
-            const uint32_t bytes = (uint32_t)cbulk * 8u;
-            mbar_arrive_expect_tx(&bar, 4u * bytes);
-            bulk_g2s(sh_h, hin + c0, bytes, &bar);
-            bulk_g2s(sh_hu, huin + c0, bytes, &bar);
-            bulk_g2s(sh_hv, hvin + c0, bytes, &bar);
-            bulk_g2s(sh_b, A.b + c0, bytes, &bar);
-        }
-        for (int i = cbulk + tid; i < cn; i += blockDim.x) {
-            sh_h[i] = hin[c0 + i];
-            sh_hu[i] = huin[c0 + i];
-            sh_hv[i] = hvin[c0 + i];
-            sh_b[i] = A.b[c0 + i];
-        }
-        if (cbulk > 0) {  // one thread waits for the copy, the others at the barrier
-            if (tid == 0) {
-                int polls = 0;
-                while (!mbar_try_wait(&bar, phase)) {
-                    if (++polls > kWaitLimit) {
-                        s_error = 2u;
-                        break;
-                    }
-                }
-            }
-            phase ^= 1u;
-        }
+        // ---- 1. the segment's state, staged in buffer kbuf
+        wait(kbuf);
         __syncthreads();
         if (s_error) break;
+        double* sh_h = stage + (size_t)kbuf * 4 * T;
+        double* sh_hu = sh_h + T;
+        double* sh_hv = sh_hu + T;
+        double* sh_b = sh_hv + T;
         for (int i = tid; i < cn; i += blockDim.x) {
             double d, sq, y;
             depth_terms(State{sh_h[i], 0.0, 0.0, sh_b[i]}, P.drytol, d, sq, y);
@@ -420,6 +453,19 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             A.flags[c] = f;
         }
         __syncthreads();
+        if (!depth2) {  // draw and stage the next segment now
+            if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+            __syncthreads();
+            seg_next = s_seg;
+            if (seg_next < A.n_seg) issue(seg_next, 0);
+        } else {
+            kbuf ^= 1;
+        }
+        seg = seg_next;
+    }
+    if (pending) {  // left early on an error: let the copies in flight land first (bounded)
+        wait(0);
+        wait(1);
     }
 
     // ---- 4. reductions and the last-CTA finalisation (post_traversal_grid_op, :111-131)

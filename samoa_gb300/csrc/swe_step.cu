@@ -232,6 +232,7 @@ struct swe_ctx {
     bool has_mesh = false, has_state = false;
     // tiling
     int32_t seg_cells = 512, block_threads = 128;  // the best of a sweep on GB300 (2^24 cells)
+    int32_t stage_depth = 1;                        // segments staged ahead per CTA (1 or 2)
     int32_t arith = SWE_ARITH_STRICT;
     int64_t n_seg = 0, n_tasks = 0;
     int grid = 0, max_ndepth = 1;
@@ -300,9 +301,14 @@ int device_alloc(void** p, size_t bytes) {
     return SWE_OK;
 }
 
-size_t smem_bytes(const swe_ctx* c) {
-    return (size_t)18 * c->seg_cells * sizeof(double) + (size_t)5 * c->max_ndepth * sizeof(double);
+size_t smem_bytes_for(int64_t seg_cells, int stage_depth, int max_ndepth) {
+    // staging [depth][4][T], RN(1/depth) and sqrt(g depth) [2][T], edge slots [12][T], depth tables [5][nd]
+    return (size_t)(14 + 4 * stage_depth) * (size_t)seg_cells * sizeof(double) + (size_t)5 * max_ndepth * sizeof(double);
 }
+
+size_t smem_bytes(const swe_ctx* c) { return smem_bytes_for(c->seg_cells, c->stage_depth, c->max_ndepth); }
+
+constexpr size_t kMaxSmem = 227 * 1024;
 
 int check_params(const swe_params* p) {
     if (!kernel_for(p->solver)) return set_error(SWE_E_INVALID, "unknown solver %d", p->solver);
@@ -537,6 +543,7 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     A.max_ndepth = c->max_ndepth;
     A.n_cells_total = (int32_t)c->cells_total;
     A.use_tma = use_tma;
+    A.stage_depth = c->stage_depth;
     A.fixed_io = 0;
     if (io) {
         A.h[0] = io[0]; A.hu[0] = io[1]; A.hv[0] = io[2];
@@ -679,11 +686,26 @@ int swe_set_tiling(swe_ctx* c, int32_t seg_cells, int32_t block_threads) {
         return set_error(SWE_E_INVALID, "segment_cells %d: need an even value in 64..1536", seg_cells);
     if (block_threads && (block_threads < 64 || block_threads > 256 || (block_threads & 31)))
         return set_error(SWE_E_INVALID, "block_threads %d: need a multiple of 32 in 64..256", block_threads);
+    if (seg_cells && smem_bytes_for(seg_cells, c->stage_depth, kMaxDepth + 1) > kMaxSmem)
+        return set_error(SWE_E_INVALID, "segment_cells %d with staging depth %d exceeds shared memory", seg_cells,
+                         c->stage_depth);
     if (seg_cells) c->seg_cells = seg_cells;
     if (block_threads) c->block_threads = block_threads;
     if (!c->has_mesh) return SWE_OK;
     cudaSetDevice(c->device);
     return rebuild_tasks(c);
+}
+
+int swe_set_staging(swe_ctx* c, int32_t depth) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (depth != 1 && depth != 2) return set_error(SWE_E_INVALID, "staging depth %d: need 1 or 2", depth);
+    if (smem_bytes_for(c->seg_cells, depth, std::max(c->max_ndepth, kMaxDepth + 1)) > kMaxSmem)
+        return set_error(SWE_E_INVALID, "staging depth %d with %d-cell segments exceeds shared memory", depth,
+                         c->seg_cells);
+    c->stage_depth = depth;
+    if (!c->has_mesh) return SWE_OK;
+    cudaSetDevice(c->device);
+    return configure_launch(c);
 }
 
 int swe_set_arith(swe_ctx* c, int32_t mode) {

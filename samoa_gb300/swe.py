@@ -179,6 +179,10 @@ class SweContext:
     def set_tiling(self, segment_cells=0, block_threads=0):
         _lib.check(self.L.swe_set_tiling(self.ptr, segment_cells, block_threads))
 
+    def set_staging(self, depth):
+        """Segments staged ahead per CTA: 1 or 2 (swe_set_staging)."""
+        _lib.check(self.L.swe_set_staging(self.ptr, int(depth)))
+
     def set_arith(self, mode):
         """"strict" (bit-exact FP64, default) or "fma" (fused multiply-adds, within a few ulps per step)."""
         _lib.check(self.L.swe_set_arith(self.ptr, {"strict": 0, "fma": 1}[mode]))
@@ -330,8 +334,10 @@ class SweEulerTimestepTraversal:
         self.ctx.set_params(cfg.params())
         self._mesh_key = None
 
-    def set_tiling(self, segment_cells=0, block_threads=0):
+    def set_tiling(self, segment_cells=0, block_threads=0, staging_depth=None):
         self.ctx.set_tiling(segment_cells, block_threads)
+        if staging_depth:
+            self.ctx.set_staging(staging_depth)
 
     def _ensure(self, grid):
         key = (id(grid.mesh), grid.mesh.version)

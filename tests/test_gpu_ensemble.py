@@ -37,12 +37,13 @@ def _upload(ens, members):
     ens.set_times([g.r_time for _, g, _ in members], [g.r_dt for _, g, _ in members])
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_ensemble_members_match_oracle(swe_lib, oracle_lib, graph):
+@pytest.mark.parametrize("graph,staging", [(False, 1), (True, 1), (False, 2)])
+def test_ensemble_members_match_oracle(swe_lib, oracle_lib, graph, staging):
     members = _ensemble_members()
     ens = swe.SweEnsemble(0)
     try:
         ens.set_tiling(128, 128)
+        ens.set_staging(staging)
         _upload(ens, members)
         refs = [omp_state(m, g) for m, g, _ in members]
         steps = 7

@@ -72,9 +72,10 @@ def test_refinement_flags_bitexact(swe_lib, oracle_lib):
     run_compare_walk(scn, 8)
 
 
-@pytest.mark.parametrize("tiling", [(64, 64), (96, 128), (1536, 256), (1024, 256), (256, 96)])
+@pytest.mark.parametrize("tiling", [(64, 64), (96, 128), (1536, 256), (1024, 256), (256, 96), (64, 64, 2),
+                                    (512, 128, 2), (1280, 256, 2)])
 def test_tilings_bitexact(swe_lib, oracle_lib, tiling):
-    """Segment length and block size change nothing in the results."""
+    """Segment length, block size and staging depth change nothing in the results."""
     scn = scenarios.parabolic_bowl(log2_cells=13, amplitude=1.0)
     run_compare_walk(scn, 6, tiling=tiling)
 
@@ -118,7 +119,7 @@ def _odd_mesh(depth):
     return swe.Mesh(m.depth[:n].copy(), m.plotter[:n].copy(), ec.copy(), el.copy(), bc, bl, m.centroids[:n].copy())
 
 
-@pytest.mark.parametrize("tiling", [(64, 64), (512, 256)])
+@pytest.mark.parametrize("tiling", [(64, 64), (512, 256), (64, 64, 2)])
 def test_odd_cell_count_against_omp(swe_lib, oracle_lib, tiling):
     mesh = _odd_mesh(9)
     assert mesh.n_cells % 2 == 1
