@@ -119,6 +119,26 @@ def _odd_mesh(depth):
     return swe.Mesh(m.depth[:n].copy(), m.plotter[:n].copy(), ec.copy(), el.copy(), bc, bl, m.centroids[:n].copy())
 
 
+def test_full_size_basin_against_omp(swe_lib, oracle_lib):
+    """The bench workload itself, 2^26 cells with the autotuned tiling (768 x 256):
+    three steps bit-exact against the OpenMP oracle, state, flags, dt."""
+    scn = scenarios.ocean_basin(log2_cells=26, steps=3, device="cuda")
+    g = scn.grid
+    S = omp_state(g.mesh, g)
+    P = oracle_params(scn.cfg)
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    trav.set_tiling(768, 256)
+    try:
+        for k in range(3):
+            S.steps(P, 1)
+            trav.traverse(g)
+            assert_state_equal("2^26 basin step %d" % k, g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+            assert np.array_equal(g.refinement, S.flags)
+            assert g.r_dt == S.scal[1] and g.r_time == S.scal[0]
+    finally:
+        trav.close()
+
+
 @pytest.mark.parametrize("tiling", [(64, 64), (512, 256), (64, 64, 2)])
 def test_odd_cell_count_against_omp(swe_lib, oracle_lib, tiling):
     mesh = _odd_mesh(9)
