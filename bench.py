@@ -489,6 +489,7 @@ def run_gpu(a, rank, world, local):
     if rank == 0:
         fp64 = fp64_dgemm_tflops(torch)
         fp64_util = profile_figure("fp64_pipe_active_pct")
+        fp64_per_cell = profile_figure("fp64_instr_per_cell")
         cpu = None
         if world == 1 and not a.no_cpu:
             from oracle import oracle as O
@@ -528,6 +529,14 @@ def run_gpu(a, rank, world, local):
             "roofline": roofline,
             "fp64": {"dgemm_tflops_measured": fp64, "fp64_pipe_active_pct_ncu": fp64_util,
                      "note": "the step is FP64-issue bound on GB300; see the ncu summary in profiles/"},
+            # the bound that sets the pace: FP64 instructions per cell (ncu) x cells/s against the FP64
+            # instruction rate of the measured DGEMM (one DFMA = 2 flops)
+            "fp64_roofline": None if not (fp64 and fp64_per_cell) else {
+                "bound": "fp64", "achieved": value * fp64_per_cell / 1e9,
+                "peak": fp64 * 1e3 / 2.0, "unit": "G FP64 instructions/s",
+                "frac": value * fp64_per_cell / 1e9 / (fp64 * 1e3 / 2.0),
+                "instr_per_cell": fp64_per_cell,
+                "source": "instr_per_cell from the ncu summary in profiles/, peak from the DGEMM measured above"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "ensemble": ensemble,
