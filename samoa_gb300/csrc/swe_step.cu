@@ -254,6 +254,9 @@ struct swe_ctx {
     int64_t dt_seq_len = 0;
     std::vector<double> dt_seq_host;
     uint8_t* branch = nullptr;      // wet/dry branch flags of the last forward step (adjoint)
+    // allocated sizes (elements) of the per-cell, per-instance and task buffers: a re-upload that
+    // fits reuses them, so remeshing every step does not pay cudaMalloc / cudaFree each time
+    size_t cap_cells = 0, cap_inst = 0, cap_tasks = 0, cap_segs = 0;
     // host mirror of the device step counter and dt-sequence base: every change
     // goes through this library (launches, graph replays, restores), so the host
     // knows the traversal parity without reading the device
@@ -276,19 +279,27 @@ void drop_graphs(swe_ctx* c) {
     c->graphs.clear();
 }
 
-void free_mesh_buffers(swe_ctx* c) {
+// Forget the mesh: graphs, the frozen dt sequence and the adjoint's branch
+// buffer always go; the cell, instance and task buffers are released only with
+// `release` (else kept for a re-upload that fits them).
+void free_mesh_buffers(swe_ctx* c, bool release = true) {
     drop_graphs(c);
+    cudaFree(c->dt_seq); cudaFree(c->branch);
+    c->branch = nullptr;
+    c->dt_seq = nullptr;
+    c->dt_seq_len = 0;
+    c->dt_seq_host.clear();
+    c->has_mesh = c->has_state = false;
+    if (!release) return;
     for (int k = 0; k < 2; ++k) {
         cudaFree(c->h[k]); cudaFree(c->hu[k]); cudaFree(c->hv[k]);
         c->h[k] = c->hu[k] = c->hv[k] = nullptr;
     }
     cudaFree(c->b); cudaFree(c->depth); cudaFree(c->flags); cudaFree(c->tasks); cudaFree(c->seg_ptr);
-    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->dt_seq); cudaFree(c->branch);
-    c->branch = nullptr;
-    c->dt_seq_host.clear();
+    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is);
     c->b = nullptr; c->depth = nullptr; c->flags = nullptr; c->tasks = nullptr; c->seg_ptr = nullptr;
-    c->seg_info = nullptr; c->ip = nullptr; c->is = nullptr; c->dt_seq = nullptr; c->dt_seq_len = 0;
-    c->has_mesh = c->has_state = false;
+    c->seg_info = nullptr; c->ip = nullptr; c->is = nullptr;
+    c->cap_cells = c->cap_inst = c->cap_tasks = c->cap_segs = 0;
 }
 
 int device_alloc(void** p, size_t bytes) {
@@ -377,20 +388,30 @@ int rebuild_tasks(swe_ctx* c) {
         int rc = build_tasks(c->mesh[(size_t)i], c->offset[(size_t)i], i, c->seg_cells, seg_ptr, seg_info, tasks);
         if (rc) return rc;
     }
-    cudaFree(c->tasks);
-    cudaFree(c->seg_ptr);
-    cudaFree(c->seg_info);
-    c->tasks = nullptr;
-    c->seg_ptr = nullptr;
-    c->seg_info = nullptr;
     c->n_seg = (int64_t)seg_info.size();
     c->adj_seg_cells = 0;  // the adjoint's grid depends on the segment count
     c->n_tasks = (int64_t)tasks.size();
     if (c->n_seg >= ((int64_t)1 << 31)) return set_error(SWE_E_INVALID, "too many segments");
     int rc;
-    if ((rc = device_alloc((void**)&c->tasks, sizeof(Task) * tasks.size()))) return rc;
-    if ((rc = device_alloc((void**)&c->seg_ptr, sizeof(long long) * seg_ptr.size()))) return rc;
-    if ((rc = device_alloc((void**)&c->seg_info, sizeof(SegInfo) * seg_info.size()))) return rc;
+    if (tasks.size() > c->cap_tasks) {
+        cudaFree(c->tasks);
+        c->tasks = nullptr;
+        c->cap_tasks = 0;
+        const size_t cap = tasks.size() + tasks.size() / 8 + 64;
+        if ((rc = device_alloc((void**)&c->tasks, sizeof(Task) * cap))) return rc;
+        c->cap_tasks = cap;
+    }
+    if (seg_info.size() + 1 > c->cap_segs) {
+        cudaFree(c->seg_ptr);
+        cudaFree(c->seg_info);
+        c->seg_ptr = nullptr;
+        c->seg_info = nullptr;
+        c->cap_segs = 0;
+        const size_t cap = seg_info.size() + seg_info.size() / 8 + 16;
+        if ((rc = device_alloc((void**)&c->seg_ptr, sizeof(long long) * (cap + 1)))) return rc;
+        if ((rc = device_alloc((void**)&c->seg_info, sizeof(SegInfo) * cap))) return rc;
+        c->cap_segs = cap;
+    }
     CUDA_TRY(cudaMemcpyAsync(c->tasks, tasks.data(), sizeof(Task) * tasks.size(), cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->seg_ptr, seg_ptr.data(), sizeof(long long) * seg_ptr.size(), cudaMemcpyHostToDevice,
                              c->stream));
@@ -423,7 +444,7 @@ int upload_meshes(swe_ctx* c, int64_t ni, const int64_t* n_cells, const int64_t*
     if (!n_cells || !n_edges || !n_bnd) return set_error(SWE_E_INVALID, "null size arrays");
     cudaSetDevice(c->device);
     CUDA_TRY(cudaStreamSynchronize(c->stream));
-    free_mesh_buffers(c);
+    free_mesh_buffers(c, false);
     std::vector<HostMesh> meshes((size_t)ni);
     std::vector<int64_t> offset((size_t)ni);
     int64_t pc = 0, pe = 0, pb = 0, off = 0;
@@ -456,16 +477,22 @@ int upload_meshes(swe_ctx* c, int64_t ni, const int64_t* n_cells, const int64_t*
     c->params.assign((size_t)ni, p0);
     const size_t n = (size_t)off;
     int rc = SWE_OK;
-    for (int k = 0; k < 2 && !rc; ++k)
-        if ((rc = device_alloc((void**)&c->h[k], n * 8)) || (rc = device_alloc((void**)&c->hu[k], n * 8)) ||
-            (rc = device_alloc((void**)&c->hv[k], n * 8)))
-            break;
-    if (!rc && !(rc = device_alloc((void**)&c->b, n * 8)) && !(rc = device_alloc((void**)&c->depth, n)) &&
-        !(rc = device_alloc((void**)&c->flags, n)) && !(rc = device_alloc((void**)&c->ip, sizeof(InstParams) * ni)))
-        rc = device_alloc((void**)&c->is, sizeof(InstScalars) * ni);
-    if (rc) {
-        free_mesh_buffers(c);
-        return rc;
+    if (n > c->cap_cells || (size_t)ni > c->cap_inst) {  // grow (with headroom for a remesh that refines)
+        free_mesh_buffers(c, true);
+        const size_t cap = n + n / 8 + 64, capi = (size_t)ni;
+        for (int k = 0; k < 2 && !rc; ++k)
+            if ((rc = device_alloc((void**)&c->h[k], cap * 8)) || (rc = device_alloc((void**)&c->hu[k], cap * 8)) ||
+                (rc = device_alloc((void**)&c->hv[k], cap * 8)))
+                break;
+        if (!rc && !(rc = device_alloc((void**)&c->b, cap * 8)) && !(rc = device_alloc((void**)&c->depth, cap)) &&
+            !(rc = device_alloc((void**)&c->flags, cap)) && !(rc = device_alloc((void**)&c->ip, sizeof(InstParams) * capi)))
+            rc = device_alloc((void**)&c->is, sizeof(InstScalars) * capi);
+        if (rc) {
+            free_mesh_buffers(c);
+            return rc;
+        }
+        c->cap_cells = cap;
+        c->cap_inst = capi;
     }
     // zero the padding cells; copy depths per instance
     for (int k = 0; k < 2; ++k) {
