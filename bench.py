@@ -299,6 +299,7 @@ def adaptive_compare(a, device):
             "steps": st["steps"], "cells_first": st["cells"][0], "cells_last": st["cells"][-1],
             "apriori_refinement_s": t_init, "step_cell_updates_per_s": st["cell_updates"] / st["step_s"],
             "remesh_s_per_step": st["remesh_s"] / max(1, st["remeshes"]),
+            "remesh_parts_s_per_step": {k: st[k + "_s"] / max(1, st["remeshes"]) for k in ("download", "adapt", "upload")},
             "step_s_per_step": st["step_s"] / st["steps"],
             "end_to_end_cell_updates_per_s": st["cell_updates"] / (st["step_s"] + st["remesh_s"]),
             "note": "remesh before every step from the previous step's flags (host C++: conformity, "

@@ -414,7 +414,8 @@ def run_adaptive(cfg, mesh, h, hu, hv, b, dt, steps, adapt_every=1, bathymetry=N
     ctx = SweContext(device)
     stream = torch.cuda.Stream(device=device)
     ctx.set_stream(stream.cuda_stream)
-    stats = {"steps": 0, "cell_updates": 0, "step_s": 0.0, "remesh_s": 0.0, "remeshes": 0, "cells": []}
+    stats = {"steps": 0, "cell_updates": 0, "step_s": 0.0, "remesh_s": 0.0, "remeshes": 0, "cells": [],
+             "download_s": 0.0, "adapt_s": 0.0, "upload_s": 0.0}
     try:
         ctx.set_params(cfg.params())
         ctx.upload_mesh(mesh)
@@ -427,6 +428,7 @@ def run_adaptive(cfg, mesh, h, hu, hv, b, dt, steps, adapt_every=1, bathymetry=N
                 t0 = _time.perf_counter()
                 h, hu, hv, b = ctx.download_state()
                 time, dt, _ = ctx.get_time()
+                t1 = _time.perf_counter()
                 new, (h, hu, hv, b), src = adapt(mesh, flags, h, hu, hv, b, with_source=True)
                 if bathymetry is not None:
                     fine = new.depth > mesh.depth[src]
@@ -435,10 +437,15 @@ def run_adaptive(cfg, mesh, h, hu, hv, b, dt, steps, adapt_every=1, bathymetry=N
                         y = cfg.scaling * new.centroids[fine, 1] + cfg.offset[1]
                         b[fine] = bathymetry(x, y)
                 mesh = new
+                t2 = _time.perf_counter()
                 ctx.upload_mesh(mesh)
                 ctx.upload_state(h, hu, hv, b)
                 ctx.set_time(time, dt)
-                stats["remesh_s"] += _time.perf_counter() - t0
+                t3 = _time.perf_counter()
+                stats["remesh_s"] += t3 - t0
+                stats["download_s"] += t1 - t0
+                stats["adapt_s"] += t2 - t1
+                stats["upload_s"] += t3 - t2
                 stats["remeshes"] += 1
             e0.record(stream)
             ctx.traverse(1)
