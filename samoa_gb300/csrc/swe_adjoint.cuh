@@ -113,7 +113,8 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double beta1 = div_rn(sE2 * delhu - dpd, rD);
     const double beta2 = div_rn(dpd - sE1 * delhu, rD);
     const double sw[3] = {sE1, 0.5 * (sE1 + sE2), sE2};
-    // ---------------- reverse
+    // ---------------- reverse (cotangents: products fused into FMAs where they feed a sum; they
+    // need no bit-exact agreement, only the forward recompute above does)
     // back-rotation p = net(2:3) T (for an axis-aligned normal: signed selections)
     double nL[3], nR[3];
     nL[0] = gL[0];
@@ -125,8 +126,8 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         nL[1] = flip(gL[2], sn); nL[2] = flip(gL[1], !sn);
         nR[1] = flip(gR[2], sn); nR[2] = flip(gR[1], !sn);
     } else {
-        nL[1] = gL[1] * n1 + gL[2] * n2; nL[2] = -gL[1] * n2 + gL[2] * n1;
-        nR[1] = gR[1] * n1 + gR[2] * n2; nR[2] = -gR[1] * n2 + gR[2] * n1;
+        nL[1] = fma(gL[1], n1, gL[2] * n2); nL[2] = fma(-gL[1], n2, gL[2] * n1);
+        nR[1] = fma(gR[1], n1, gR[2] * n2); nR[2] = fma(-gR[1], n2, gR[2] * n1);
     }
     // net-update split by wave-speed sign; walls remove waves
     double F[3][3];
@@ -143,17 +144,17 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     // fw(3,2) = ((huR vR - huL vL) - fw(3,1)) - fw(3,3); wave 2 carries no h / hu
     double b_huR = F[2][1] * vR, b_vR = F[2][1] * huR, b_huL = -F[2][1] * vL, b_vL = -F[2][1] * huL;
     const double F30 = F[2][0] - F[2][1], F32 = F[2][2] - F[2][1];
-    double b_beta1 = F[0][0] + F[1][0] * sE1 + F30 * vL;
-    double b_beta2 = F[0][2] + F[1][2] * sE2 + F32 * vR;
+    double b_beta1 = fma(F30, vL, fma(F[1][0], sE1, F[0][0]));
+    double b_beta2 = fma(F32, vR, fma(F[1][2], sE2, F[0][2]));
     double b_sE1 = F[1][0] * beta1, b_sE2 = F[1][2] * beta2;
-    b_vL += F30 * beta1;
-    b_vR += F32 * beta2;
+    b_vL = fma(F30, beta1, b_vL);
+    b_vR = fma(F32, beta2, b_vR);
     // beta1 = (sE2 delhu - dpd) / D, beta2 = (dpd - sE1 delhu) / D, D = sE2 - sE1
     const double N1b = b_beta1 * rD.y, N2b = b_beta2 * rD.y;
-    const double b_D = -(b_beta1 * beta1 + b_beta2 * beta2) * rD.y;
-    b_sE2 += N1b * delhu + b_D;
-    b_sE1 += -N2b * delhu - b_D;
-    double b_delhu = N1b * sE2 - N2b * sE1;
+    const double b_D = -fma(b_beta1, beta1, b_beta2 * beta2) * rD.y;
+    b_sE2 += fma(N1b, delhu, b_D);
+    b_sE1 -= fma(N2b, delhu, b_D);
+    double b_delhu = fma(N1b, sE2, -(N2b * sE1));
     const double b_dpd = N2b - N1b;
     // dpd = delphi - ddp, ddp = -(K dB), K = c Hs
     double b_delphi = b_dpd;
@@ -169,26 +170,27 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     double b_sR = e2_is_sR ? b_sE2 : 0.0, b_r2 = e2_is_sR ? 0.0 : b_sE2;
     const double b_uhat = b_r1 + b_r2;
     const double b_chat = b_r2 - b_r1;
-    if (chat > 0.0) b_Hs += b_chat * (0.5 * rcp_nr(chat)) * (g * 0.5);
+    if (chat > 0.0) b_Hs = fma(b_chat * (0.5 * rcp_nr(chat)), g * 0.5, b_Hs);
     double b_uL = b_sL, b_uR = b_sR;
     double b_sqL = -b_sL, b_sqR = b_sR;
     const double b_A = b_uhat * rB.y, b_B = -b_uhat * uhat * rB.y;
-    b_sqL += b_A * uL + b_B;
-    b_sqR += b_A * uR + b_B;
-    b_uL += b_A * sqL;
-    b_uR += b_A * sqR;
+    b_sqL += fma(b_A, uL, b_B);
+    b_sqR += fma(b_A, uR, b_B);
+    b_uL = fma(b_A, sqL, b_uL);
+    b_uR = fma(b_A, sqR, b_uR);
     // delphi = ((T1 - T2) + T3) - T4
     {
         const double d = b_delphi;
         const double su = uL + uR, dhu = huR - huL, uu = uL * uR, dh = hR - hL;
-        b_huR += d * su;
-        b_huL -= d * su;
-        b_uL += d * dhu - d * uR * dh;
-        b_uR += d * dhu - d * uL * dh;
+        const double dsu = d * su;
+        b_huR += dsu;
+        b_huL -= dsu;
+        b_uL += fma(d, dhu, -(d * uR * dh));
+        b_uR += fma(d, dhu, -(d * uL * dh));
         double b_hR = -d * uu, b_hL = d * uu;
         const double b_X = d * c * Hs;
-        b_Hs += d * (c * X) - d * c * dB;
-        b_dB += -d * (c * Hs);
+        b_Hs += fma(d, c * X, -(d * c * dB));
+        b_dB = fma(-d, c * Hs, b_dB);
         // X = ((bR + hR) - bL) - hL
         double b_bR = b_X, b_bL = -b_X;
         b_hR += b_X;
@@ -199,8 +201,8 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         b_bR += b_dB;
         b_bL -= b_dB;
         // sqrt(g h) of the fixed-up depths
-        if (sqL > 0.0) b_hL += b_sqL * (0.5 * g * rcp_nr(sqL));
-        if (sqR > 0.0) b_hR += b_sqR * (0.5 * g * rcp_nr(sqR));
+        if (sqL > 0.0) b_hL = fma(b_sqL, 0.5 * g * rcp_nr(sqL), b_hL);
+        if (sqR > 0.0) b_hR = fma(b_sqR, 0.5 * g * rcp_nr(sqR), b_hR);
         // undo the wall / lowering fix-ups: map the cotangents back to the original sides
         double b_hL0 = 0.0, b_hR0 = 0.0, b_bL0 = 0.0, b_bR0 = 0.0;
         if (wall_r) {  // hR = hL, huR = -huL, bR = bL, uR = -uL, vR = vL
@@ -230,14 +232,14 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         // wet extraction: u = hu / h, v = hv / h on wet sides; dry sides are constants
         double b_pL1 = 0.0, b_pL2 = 0.0, b_pR1 = 0.0, b_pR2 = 0.0;
         if (wetR) {
-            b_pR1 += b_huR + b_uR * yR0;
-            b_pR2 += b_vR * yR0;
-            b_hR0 = b_hR - (b_uR * uR + b_vR * vR) * yR0;
+            b_pR1 += fma(b_uR, yR0, b_huR);
+            b_pR2 = fma(b_vR, yR0, b_pR2);
+            b_hR0 = fma(-fma(b_uR, uR, b_vR * vR), yR0, b_hR);
         }
         if (wetL) {
-            b_pL1 += b_huL + b_uL * yL0;
-            b_pL2 += b_vL * yL0;
-            b_hL0 = b_hL - (b_uL * uL + b_vL * vL) * yL0;
+            b_pL1 += fma(b_uL, yL0, b_huL);
+            b_pL2 = fma(b_vL, yL0, b_pL2);
+            b_hL0 = fma(-fma(b_uL, uL, b_vL * vL), yL0, b_hL);
         }
         // depths h - b, rotations p_edge = T p
         outL.h += b_hL0;
@@ -251,10 +253,10 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
             outL.hu += flip(b_pL2, !sn); outL.hv += flip(b_pL1, sn);
             outR.hu += flip(b_pR2, !sn); outR.hv += flip(b_pR1, sn);
         } else {
-            outL.hu += b_pL1 * n1 - b_pL2 * n2;
-            outL.hv += b_pL1 * n2 + b_pL2 * n1;
-            outR.hu += b_pR1 * n1 - b_pR2 * n2;
-            outR.hv += b_pR1 * n2 + b_pR2 * n1;
+            outL.hu += fma(b_pL1, n1, -(b_pL2 * n2));
+            outL.hv += fma(b_pL1, n2, b_pL2 * n1);
+            outR.hu += fma(b_pR1, n1, -(b_pR2 * n2));
+            outR.hv += fma(b_pR1, n2, b_pR2 * n1);
         }
     }
 }
