@@ -142,6 +142,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def host_cpu():
+    """The host CPU's model name and logical core count (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() in ("Model name", "Model"):
+                model = line.split(":", 1)[1].strip()
+                if not model.isdigit():
+                    break
+    except Exception:
+        pass
+    return {"model": model, "logical_cores": os.cpu_count()}
+
+
 def cpu_baseline(log2, steps, solver, threads):
     """Time the OpenMP CPU step (the oracle's restatement of the reference step)
     on a 2^log2-cell sample of the same basin workload."""
@@ -196,7 +211,8 @@ def run_reference(a, rank, world):
         "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "solver": a.solver,
                    "sample_cells": m.n_cells},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "host": host_cpu()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -496,7 +512,7 @@ def run_gpu(a, rank, world, local):
             from oracle import oracle as O
             threads = O.max_threads()
             v, t = cpu_baseline(a.cpu_sample_log2, a.cpu_steps, a.solver, threads)
-            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "host": host_cpu(),
                    "sample": "2^%d-cell sample of the same basin, %d steps (%.1f s), OpenMP C restatement of the "
                              "reference step" % (a.cpu_sample_log2, a.cpu_steps, t)}
         ensemble = None

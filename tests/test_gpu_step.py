@@ -174,6 +174,25 @@ def test_lake_at_rest_is_exact(swe_lib):
         trav.close()
 
 
+@pytest.mark.parametrize("solver", ["fwave", "aug_riemann", "llfbath"])
+def test_all_dry_domain(swe_lib, oracle_lib, solver):
+    """Dry land everywhere (surface at min(b, 0) below a positive bottom): no edge
+    carries a flux, the state stays as it is, every flag is bit-exact with the
+    oracle walk and dt_new stays at its initial huge value."""
+    d = 9
+    mesh = swe.uniform_mesh(d)
+    cfg = swe.Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=0.01,
+                     scaling=1.0, offset=(-0.5, -0.5), i_min_depth=d, i_max_depth=d + 1)
+    rng = np.random.default_rng(31)
+    b = 1.0 + rng.random(mesh.n_cells)
+    h = np.minimum(b, 0.0)
+    g = swe.Grid(mesh, h.copy(), np.zeros(mesh.n_cells), np.zeros(mesh.n_cells), b, 0.0, 1e-3)
+    scn = scenarios.Scenario("all_dry", g, cfg, 3)
+    run_compare_walk(scn, 3)
+    assert np.array_equal(g.h, h) and not g.hu.any() and not g.hv.any()
+    assert g.r_dt_new == np.finfo(np.float64).max
+
+
 def test_mass_conservation_and_drift(swe_lib, oracle_lib):
     """Mass is conserved to round-off (reflective walls, no wet/dry clamps);
     after 1,000 steps the GPU state still equals the oracle's bit for bit."""
