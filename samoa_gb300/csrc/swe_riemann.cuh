@@ -498,15 +498,30 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
 // axis-aligned normal each component of T p and of net(2:3) T is one exact
 // product plus a signed zero, i.e. the other momentum with its sign flipped
 // and -0 mapped to +0, which integer instructions give bit for bit while the
-// operands are finite (0 * inf would be NaN); otherwise the general form runs.
+// operands are finite (0 * inf would be NaN). For a diagonal normal
+// (|n1| = |n2| = c) the four products of each rotation are +-RN(c p1) and
+// +-RN(c p2), since RN(-x) = -RN(x): two products per side, the signs set on
+// the bit patterns. Otherwise the general form runs.
 template <int SOLVER>
 __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR, double dL,
                                              double dR, double sqL, double sqR, double yL, double yR,
                                              double drytol, Update& fL, Update& fR, int axis = 0) {
-    const bool fast = axis != 0 && is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
+    const bool fin = is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
+    const bool fast = axis != 0 && fin;
+    const bool diag = axis == 0 && fin && abs_bits(n1) == abs_bits(n2);
     const bool sn = axis == 1 ? lt0(n1) : lt0(n2);  // sign of the nonzero component
+    const bool g1 = dbits(n1) < 0, g2 = dbits(n2) < 0;  // sign bits of the normal
+    const double c = bitsd(abs_bits(n1));
     double pL1, pL2, pR1, pR2;
-    if (fast) {
+    if (diag) {
+        // RN(n1 p1) = +-a1, RN(n2 p2) = +-a2, RN(-n2 p1) = -+a1, RN(n1 p2) = +-a2
+        const double aL1 = imul_rot(c, QL.p1), aL2 = imul_rot(c, QL.p2);
+        const double aR1 = imul_rot(c, QR.p1), aR2 = imul_rot(c, QR.p2);
+        pL1 = z0(flip(aL1, g1)) + flip(aL2, g2);
+        pL2 = z0(flip(aL1, !g2)) + flip(aL2, g1);
+        pR1 = z0(flip(aR1, g1)) + flip(aR2, g2);
+        pR2 = z0(flip(aR1, !g2)) + flip(aR2, g1);
+    } else if (fast) {
         if (axis == 1) {
             pL1 = z0(flip(QL.p1, sn)); pL2 = z0(flip(QL.p2, sn));
             pR1 = z0(flip(QR.p1, sn)); pR2 = z0(flip(QR.p2, sn));
@@ -527,7 +542,16 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
     fL.s = ms;
     fR.h = netR[0];
     fR.s = ms;
-    if (fast && is_finite(netL[1]) && is_finite(netL[2]) && is_finite(netR[1]) && is_finite(netR[2])) {
+    const bool nfin = is_finite(netL[1]) && is_finite(netL[2]) && is_finite(netR[1]) && is_finite(netR[2]);
+    if (diag && nfin) {
+        // RN(m1 n1) = +-b1, RN(m2 (-n2)) = -+b2, RN(m1 n2) = +-b1, RN(m2 n1) = +-b2
+        const double bL1 = imul_rot(netL[1], c), bL2 = imul_rot(netL[2], c);
+        const double bR1 = imul_rot(netR[1], c), bR2 = imul_rot(netR[2], c);
+        fL.p1 = z0(flip(bL1, g1)) + flip(bL2, !g2);
+        fL.p2 = z0(flip(bL1, g2)) + flip(bL2, g1);
+        fR.p1 = z0(flip(bR1, g1)) + flip(bR2, !g2);
+        fR.p2 = z0(flip(bR1, g2)) + flip(bR2, g1);
+    } else if (fast && nfin) {
         if (axis == 1) {
             fL.p1 = z0(flip(netL[1], sn)); fL.p2 = z0(flip(netL[2], sn));
             fR.p1 = z0(flip(netR[1], sn)); fR.p2 = z0(flip(netR[2], sn));

@@ -178,11 +178,16 @@ def test_lake_at_rest_is_exact(swe_lib):
 def test_all_dry_domain(swe_lib, oracle_lib, solver):
     """Dry land everywhere (surface at min(b, 0) below a positive bottom): no edge
     carries a flux, the state stays as it is, every flag is bit-exact with the
-    oracle walk and dt_new stays at its initial huge value."""
+    oracle walk and dt_new stays at its initial huge value.
+
+    dt is clamped by r_max_time (pre_traversal_grid_op,
+    src/SWE/SWE_euler_timestep.f90:93-95): without it the step after the first
+    runs with dt = courant * huge, -dt / volume overflows to -inf and the zero
+    updates turn into NaN, in the reference as here."""
     d = 9
     mesh = swe.uniform_mesh(d)
     cfg = swe.Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=0.01,
-                     scaling=1.0, offset=(-0.5, -0.5), i_min_depth=d, i_max_depth=d + 1)
+                     scaling=1.0, offset=(-0.5, -0.5), i_min_depth=d, i_max_depth=d + 1, r_max_time=1.0)
     rng = np.random.default_rng(31)
     b = 1.0 + rng.random(mesh.n_cells)
     h = np.minimum(b, 0.0)
