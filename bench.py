@@ -418,6 +418,7 @@ def run_gpu(a, rank, world, local):
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
     tiling = ctx.get_tiling()
+    counts = ctx.task_counts()
 
     # warm-up
     ctx.traverse(a.warmup)
@@ -500,6 +501,8 @@ def run_gpu(a, rank, world, local):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic_per_cell * n if traffic_per_cell else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (%s)" % peak_kind,
+                "kernels": "step_kernel, after cross_edges_kernel for the edges between two segments; "
+                           "achieved over the time of both per step",
                 "algorithmic_bytes_per_cell": BYTES_PER_CELL}
 
     out = None
@@ -540,7 +543,7 @@ def run_gpu(a, rank, world, local):
             "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "cells": n,
                        "solver": a.solver, "boundary": "outflow", "segment_cells": tiling[0],
                        "block_threads": tiling[1], "staging_depth": tuning["best"][2] if tuning else 1,
-                       "arith": a.arith, "autotune": tuning,
+                       "arith": a.arith, "autotune": tuning, "cross_segment_edges": counts["cross_edges"],
                        "l2": "inputs larger than L2 (2.1 GB state)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline,
@@ -559,7 +562,7 @@ def run_gpu(a, rank, world, local):
             "ensemble": ensemble,
             "adjoint": adj,
             "adaptive": adaptive,
-            "gpu_launches": a.steps,
+            "gpu_launches": a.steps * counts["launches_per_step"],
             "clocks": clk,
             "sim": {"time": sim_time, "dt": dt},
         }

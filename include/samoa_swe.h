@@ -162,6 +162,14 @@ int swe_set_staging(swe_ctx* ctx, int32_t depth);
 int swe_set_arith(swe_ctx* ctx, int32_t mode);
 int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads);
 
+/* Sizes of the uploaded mesh's work lists: segments, edge tasks in the segment
+ * lists (an edge between two segments counted once per segment), edges between
+ * two segments (computed once per step by a pass before the step kernel) and
+ * kernel launches per step (1, or 2 with that pass). Any pointer may be null.
+ * No reference counterpart (the reference's sections, src/SFC_edge_traversal.f90). */
+int swe_get_task_counts(swe_ctx* ctx, int64_t* n_segments, int64_t* n_tasks, int64_t* n_cross_edges,
+                        int32_t* launches_per_step);
+
 /* Vertices of the cells of swe_mesh_uniform(depth) in the unit square, in the
  * same cell order: vertices[6 k + 2 v + {0, 1}] = (x, y) of vertex v of cell k
  * (exact dyadic values). The node coordinates samoa_get_grid hands out

@@ -35,10 +35,19 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double g = kG;
     const double c = 0.5 * g;
     // ---------------- forward (geoclaw_flux<FWAVE>, the same values)
-    const bool fast = axis != 0 && is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
+    const bool fin = is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
+    const bool fast = axis != 0 && fin;
     const bool sn = axis == 1 ? lt0(n1) : lt0(n2);
     double pL1, pL2, pR1, pR2;
-    if (fast) {
+    if (axis == 0 && fin && abs_bits(n1) == abs_bits(n2)) {  // diagonal: two products per side
+        const bool g1 = dbits(n1) < 0, g2 = dbits(n2) < 0;
+        const double cn = bitsd(abs_bits(n1));
+        const double aL1 = cn * QL.p1, aL2 = cn * QL.p2, aR1 = cn * QR.p1, aR2 = cn * QR.p2;
+        pL1 = z0(flip(aL1, g1)) + flip(aL2, g2);
+        pL2 = z0(flip(aL1, !g2)) + flip(aL2, g1);
+        pR1 = z0(flip(aR1, g1)) + flip(aR2, g2);
+        pR2 = z0(flip(aR1, !g2)) + flip(aR2, g1);
+    } else if (fast) {
         if (axis == 1) {
             pL1 = z0(flip(QL.p1, sn)); pL2 = z0(flip(QL.p2, sn));
             pR1 = z0(flip(QR.p1, sn)); pR2 = z0(flip(QR.p2, sn));

@@ -17,7 +17,12 @@ constexpr int kMaxDepth = 60;  // bit_size(int64) - 4, src/SFC_data_types.f90:77
 //   meta: bits 0-1 local edge index of a (0..2), bits 2-3 of b,
 //         bits 4-8 plotter type of a + 8, bits 9-13 of b + 8, bit 14 boundary,
 //         bits 15-16 normal direction: 0 diagonal, 1 along x, 2 along y (the
-//         same for both cells: their normals are opposite).
+//         same for both cells: their normals are opposite), bit 17 halo.
+//   pad: in a segment's list, a halo task (an edge whose other cell lies in
+//        another segment) holds the edge's index in the cross-edge list, whose
+//        pass computes both sides' updates once; in the cross-edge list, the
+//        instance.
+constexpr uint32_t kHaloBit = 1u << 17;
 struct alignas(16) Task {
     int32_t a, b;
     uint32_t meta;
@@ -104,13 +109,16 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
 int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
                 const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
                 const int8_t* bnd_local);
-// Segment descriptor: cells [c0, c0 + cn) of instance `inst`.
+// Segment descriptor: cells [c0, c0 + cn) of instance `inst`; the last `halo`
+// tasks of its list are halo tasks.
 struct alignas(16) SegInfo {
-    int32_t c0, cn, inst, pad;
+    int32_t c0, cn, inst, halo;
 };
 
+// Edge tasks of one instance's segments (appended to seg_ptr / seg_info /
+// tasks) and its cross-segment edges (appended to xtasks).
 int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t seg_cells, std::vector<int64_t>& seg_ptr,
-                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks);
+                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks, std::vector<Task>& xtasks);
 
 // Geometry tables restating src/SFC_data_types.f90:509-700 (host side, exact).
 void geometry_tables(double leg[kMaxDepth + 2], double vol[kMaxDepth + 1], double normal[17][3][2]);

@@ -54,7 +54,10 @@ struct StepArgs {
     int8_t* flags;
     const int4* tasks;
     const long long* seg_ptr;
-    const int4* seg_info;      // {first cell, cells, instance, 0}
+    const int4* seg_info;      // {first cell, cells, instance, halo tasks at the end of its list}
+    const int4* xtasks;        // cross-segment edges (Task layout, pad = instance)
+    double* xflux;             // [n_xtasks][cell a, cell b][h, hu, hv, max wave speed] of the current step
+    long long n_xtasks;
     const InstParams* ip;
     InstScalars* is;
     GlobalScalars* gs;
@@ -179,6 +182,52 @@ __device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, doub
     dtmin = DBL_MAX;
     dskey = 0;
     nref = 0;
+}
+
+// The edges between two segments, one thread each, before the step kernel:
+// the same flux as the step kernel's edge tasks (orientation by the step's
+// parity, pre-update states), both sides' updates stored by cell (a, then b).
+template <int SOLVER>
+__global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.n_xtasks) return;
+    const long long step = A.gs->step;
+    const int odd = (int)(step & 1);
+    const int ib = A.fixed_io ? 0 : odd;
+    const double* hin = A.h[ib];
+    const double* huin = A.hu[ib];
+    const double* hvin = A.hv[ib];
+    const int4 tk = __ldg(&A.xtasks[j]);
+    const uint32_t meta = (uint32_t)tk.z;
+    int L, R, iL, pL;
+    if (!odd) {
+        L = tk.x; iL = meta & 3u; pL = (meta >> 4) & 31u;
+        R = tk.y;
+    } else {
+        L = tk.y; iL = (meta >> 2) & 3u; pL = (meta >> 9) & 31u;
+        R = tk.x;
+    }
+    if ((unsigned)L >= (unsigned)A.n_cells_total || (unsigned)R >= (unsigned)A.n_cells_total || iL > 2 ||
+        pL > 16 || (unsigned)tk.w >= (unsigned)A.n_inst || ((meta >> 14) & 1u)) {
+        atomicOr(&A.gs->error, 1u);
+        return;
+    }
+    const double drytol = A.ip[tk.w].drytol;
+    const double n1 = c_normal[pL][iL][0], n2 = c_normal[pL][iL][1];
+    const State QL{hin[L], huin[L], hvin[L], A.b[L]};
+    const State QR{hin[R], huin[R], hvin[R], A.b[R]};
+    double dL, dR, sqL, sqR, yL, yR;
+    depth_terms(QL, drytol, dL, sqL, yL);
+    depth_terms(QR, drytol, dR, sqR, yR);
+    Update fL, fR;
+    edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, (int)((meta >> 15) & 3u));
+    const Update& ua = odd ? fR : fL;
+    const Update& ub = odd ? fL : fR;
+    double2* out = reinterpret_cast<double2*>(A.xflux + 8 * j);
+    out[0] = make_double2(ua.h, ua.p1);
+    out[1] = make_double2(ua.p2, ua.s);
+    out[2] = make_double2(ub.h, ub.p1);
+    out[3] = make_double2(ub.p2, ub.s);
 }
 
 template <int SOLVER>
@@ -324,11 +373,33 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             sh_rh[i] = y;
             sh_sq[i] = sq;
         }
+        // halo tasks: the cross-edge pass computed these edges' updates; copy
+        // this segment's side into its slot
+        const long long t0 = A.seg_ptr[seg], t1 = A.seg_ptr[seg + 1];
+        const long long tm = t1 - min((long long)max(si.w, 0), t1 - t0);
+        for (long long t = tm + tid; t < t1; t += blockDim.x) {
+            const int4 tk = __ldg(&A.tasks[t]);
+            const uint32_t meta = (uint32_t)tk.z;
+            const int sa = tk.x - c0;
+            const bool ain = (unsigned)sa < (unsigned)cn;
+            const int cl = ain ? sa : tk.y - c0;
+            const int le = ain ? (int)(meta & 3u) : (int)((meta >> 2) & 3u);
+            if ((unsigned)cl >= (unsigned)cn || le > 2 || !(meta & (1u << 17)) ||
+                (unsigned long long)(unsigned)tk.w >= (unsigned long long)A.n_xtasks) {
+                atomicOr(&s_error, 1u);
+                continue;
+            }
+            const double2* u = reinterpret_cast<const double2*>(A.xflux + 8 * (long long)(unsigned)tk.w + (ain ? 0 : 4));
+            const double2 u0 = u[0], u1 = u[1];
+            upd[(0 * 3 + le) * T + cl] = u0.x;
+            upd[(1 * 3 + le) * T + cl] = u0.y;
+            upd[(2 * 3 + le) * T + cl] = u1.x;
+            upd[(3 * 3 + le) * T + cl] = u1.y;
+        }
         __syncthreads();
 
         // ---- 2. edge tasks (skeleton_scalar_op / bnd_skeleton_scalar_op, :196-255)
-        const long long t0 = A.seg_ptr[seg], t1 = A.seg_ptr[seg + 1];
-        for (long long t = t0 + tid; t < t1; t += blockDim.x) {
+        for (long long t = t0 + tid; t < tm; t += blockDim.x) {
             const int4 tk = __ldg(&A.tasks[t]);
             const uint32_t meta = (uint32_t)tk.z;
             const bool bnd = (meta >> 14) & 1u;
@@ -418,8 +489,8 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             } else if (d > P.min_depth && nrm < __double_as_longlong(P.thr_coarsen)) {
                 f = -1;
             }
-            if (P.dt_by_max) {  // ds >= 0, so its bits order like its value
-                const unsigned long long x = (unsigned long long)dbits(imul_cell(ds, tab_pow[di]));
+            if (P.dt_by_max) {  // ds >= 0, so its bits order like its value; RN(ds * 2^(d+1))
+                const unsigned long long x = (unsigned long long)dbits(scale_pow2(ds, d + 1, tab_pow[di]));
                 dskey = x > dskey ? x : dskey;
             } else {
                 dtmin = dmn(dtmin, tab_vol[di] / ds);

@@ -254,7 +254,7 @@ static int normal_axis(int p, int k) {
 }
 
 int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std::vector<int64_t>& seg_ptr,
-                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks) {
+                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks, std::vector<Task>& xtasks) {
     const int64_t n = m.n_cells;
     const int64_t nseg = (n + T - 1) / T;
     if (seg_ptr.empty()) seg_ptr.push_back(0);
@@ -274,10 +274,9 @@ int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std:
         si.c0 = (int32_t)(offset + s * T);
         si.cn = (int32_t)std::min<int64_t>(T, n - s * T);
         si.inst = inst;
-        si.pad = 0;
+        si.halo = 0;
         seg_info.push_back(si);
     }
-    (void)s0;
     tasks.resize((size_t)(base + count[(size_t)nseg]));
     std::vector<int64_t> fill(count.begin(), count.end() - 1);
     for (auto& f : fill) f += base;
@@ -300,14 +299,30 @@ int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std:
                            normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1));
         t.pad = 0;
         int64_t sa = a / T, sb = b / T;
-        tasks[(size_t)fill[(size_t)sa]++] = t;
-        if (sb != sa) tasks[(size_t)fill[(size_t)sb]++] = t;
+        if (sb == sa) {
+            tasks[(size_t)fill[(size_t)sa]++] = t;
+            continue;
+        }
+        // an edge between two segments: computed once by the cross-edge pass,
+        // each segment copies its own side's update
+        if (xtasks.size() >= ((size_t)1 << 31)) return set_error(SWE_E_INVALID, "too many cross-segment edges");
+        Task h = t;
+        h.meta |= kHaloBit;
+        h.pad = (uint32_t)xtasks.size();
+        t.pad = (uint32_t)inst;
+        xtasks.push_back(t);
+        tasks[(size_t)fill[(size_t)sa]++] = h;
+        tasks[(size_t)fill[(size_t)sb]++] = h;
+        seg_info[s0 + (size_t)sa].halo++;
+        seg_info[s0 + (size_t)sb].halo++;
     }
-    // within a segment, diagonal edges first, then the axis-aligned ones, so a
-    // warp's tasks mostly take the same branch of the flux's rotation
+    // within a segment: the edges to compute, diagonal ones first, then the
+    // axis-aligned ones (so a warp's tasks mostly take the same branch of the
+    // flux's rotation), then the halo tasks
     for (int64_t s = 0; s < nseg; ++s) {
         auto first = tasks.begin() + (base + count[(size_t)s]), last = tasks.begin() + (base + count[(size_t)s + 1]);
-        std::stable_partition(first, last, [](const Task& t) { return ((t.meta >> 15) & 3u) == 0; });
+        auto mid = std::stable_partition(first, last, [](const Task& t) { return !(t.meta & kHaloBit); });
+        std::stable_partition(first, mid, [](const Task& t) { return ((t.meta >> 15) & 3u) == 0; });
     }
     return SWE_OK;
 }

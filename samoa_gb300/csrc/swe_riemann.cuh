@@ -145,6 +145,23 @@ __device__ __forceinline__ double imax(double a, double b) { return lt(b, a) ? a
 __device__ __forceinline__ double flip(double x, bool neg) {
     return bitsd(dbits(x) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
 }
+// An FP64 multiply the compiler keeps inside the branch it is written in.
+__device__ __forceinline__ double mul_here(double a, double b) {
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+// RN(x * p) for p = 2^k: while x and the result are normal numbers the product
+// is exact and only the exponent field moves (an integer add on the bit
+// pattern); +-0 stays itself; a subnormal, infinite or NaN operand and an
+// under- or overflowing result take the FP64 multiply.
+__device__ __forceinline__ double scale_pow2(double x, int k, double p) {
+    const long long b = dbits(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if ((unsigned)(e - 1) <= 2045u && (unsigned)(e + k - 1) <= 2045u) return bitsd(b + ((long long)k << 52));
+    if ((b << 1) == 0) return x;
+    return mul_here(x, p);
+}
 
 // ---------------------------------------------------------------------------
 // Correctly rounded division with a shared reciprocal.
@@ -438,7 +455,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         const Recip rD = recip_rn(sE2 - sE1);
         double beta1 = div_rn(imul(sE2, delhu) - dpd, rD);
         double beta2 = div_rn(dpd - imul(sE1, delhu), rD);
-        sw[0] = sE1; sw[1] = imul(0.5, sE1 + sE2); sw[2] = sE2;
+        sw[0] = sE1; sw[1] = scale_pow2(sE1 + sE2, -1, 0.5); sw[2] = sE2;
         fw[0][0] = beta1; fw[1][0] = imul(beta1, sE1); fw[2][0] = imul(beta1, vL);
         fw[0][2] = beta2; fw[1][2] = imul(beta2, sE2); fw[2][2] = imul(beta2, vR);
         fw[0][1] = 0.0; fw[1][1] = 0.0;

@@ -200,7 +200,20 @@ static StepKernel kernel_for(int solver) {
     }
 }
 
+static void* cross_kernel_for(int solver) {
+    switch (solver) {
+        case FWAVE: return (void*)cross_edges_kernel<FWAVE>;
+        case AUG_RIEMANN: return (void*)cross_edges_kernel<AUG_RIEMANN>;
+        case LF: return (void*)cross_edges_kernel<LF>;
+        case LF_BATH: return (void*)cross_edges_kernel<LF_BATH>;
+        case LLF: return (void*)cross_edges_kernel<LLF>;
+        case LLF_BATH: return (void*)cross_edges_kernel<LLF_BATH>;
+        default: return nullptr;
+    }
+}
+
 void* fma_step_kernel(int solver);
+void* fma_cross_kernel(int solver);
 cudaError_t fma_upload_tables();
 
 static int upload_tables() {
@@ -245,6 +258,9 @@ struct swe_ctx {
     int8_t* depth = nullptr;
     int8_t* flags = nullptr;
     Task* tasks = nullptr;
+    Task* xtasks = nullptr;         // cross-segment edges
+    double* xflux = nullptr;        // their updates, [n_xtasks][2][4]
+    int64_t n_xtasks = 0;
     long long* seg_ptr = nullptr;
     SegInfo* seg_info = nullptr;
     InstParams* ip = nullptr;
@@ -256,7 +272,7 @@ struct swe_ctx {
     uint8_t* branch = nullptr;      // wet/dry branch flags of the last forward step (adjoint)
     // allocated sizes (elements) of the per-cell, per-instance and task buffers: a re-upload that
     // fits reuses them, so remeshing every step does not pay cudaMalloc / cudaFree each time
-    size_t cap_cells = 0, cap_inst = 0, cap_tasks = 0, cap_segs = 0;
+    size_t cap_cells = 0, cap_inst = 0, cap_tasks = 0, cap_segs = 0, cap_xtasks = 0;
     // host mirror of the device step counter and dt-sequence base: every change
     // goes through this library (launches, graph replays, restores), so the host
     // knows the traversal parity without reading the device
@@ -296,10 +312,11 @@ void free_mesh_buffers(swe_ctx* c, bool release = true) {
         c->h[k] = c->hu[k] = c->hv[k] = nullptr;
     }
     cudaFree(c->b); cudaFree(c->depth); cudaFree(c->flags); cudaFree(c->tasks); cudaFree(c->seg_ptr);
-    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is);
+    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->xtasks); cudaFree(c->xflux);
     c->b = nullptr; c->depth = nullptr; c->flags = nullptr; c->tasks = nullptr; c->seg_ptr = nullptr;
-    c->seg_info = nullptr; c->ip = nullptr; c->is = nullptr;
-    c->cap_cells = c->cap_inst = c->cap_tasks = c->cap_segs = 0;
+    c->seg_info = nullptr; c->ip = nullptr; c->is = nullptr; c->xtasks = nullptr; c->xflux = nullptr;
+    c->n_xtasks = 0;
+    c->cap_cells = c->cap_inst = c->cap_tasks = c->cap_segs = c->cap_xtasks = 0;
 }
 
 int device_alloc(void** p, size_t bytes) {
@@ -383,11 +400,13 @@ int configure_launch(swe_ctx* c) {
 int rebuild_tasks(swe_ctx* c) {
     std::vector<int64_t> seg_ptr;
     std::vector<SegInfo> seg_info;
-    std::vector<Task> tasks;
+    std::vector<Task> tasks, xtasks;
     for (int i = 0; i < n_inst(c); ++i) {
-        int rc = build_tasks(c->mesh[(size_t)i], c->offset[(size_t)i], i, c->seg_cells, seg_ptr, seg_info, tasks);
+        int rc = build_tasks(c->mesh[(size_t)i], c->offset[(size_t)i], i, c->seg_cells, seg_ptr, seg_info, tasks,
+                             xtasks);
         if (rc) return rc;
     }
+    c->n_xtasks = (int64_t)xtasks.size();
     c->n_seg = (int64_t)seg_info.size();
     c->adj_seg_cells = 0;  // the adjoint's grid depends on the segment count
     c->n_tasks = (int64_t)tasks.size();
@@ -412,7 +431,21 @@ int rebuild_tasks(swe_ctx* c) {
         if ((rc = device_alloc((void**)&c->seg_info, sizeof(SegInfo) * cap))) return rc;
         c->cap_segs = cap;
     }
+    if (xtasks.size() > c->cap_xtasks) {
+        cudaFree(c->xtasks);
+        cudaFree(c->xflux);
+        c->xtasks = nullptr;
+        c->xflux = nullptr;
+        c->cap_xtasks = 0;
+        const size_t cap = xtasks.size() + xtasks.size() / 8 + 64;
+        if ((rc = device_alloc((void**)&c->xtasks, sizeof(Task) * cap))) return rc;
+        if ((rc = device_alloc((void**)&c->xflux, 8 * sizeof(double) * cap))) return rc;
+        c->cap_xtasks = cap;
+    }
     CUDA_TRY(cudaMemcpyAsync(c->tasks, tasks.data(), sizeof(Task) * tasks.size(), cudaMemcpyHostToDevice, c->stream));
+    if (!xtasks.empty())
+        CUDA_TRY(cudaMemcpyAsync(c->xtasks, xtasks.data(), sizeof(Task) * xtasks.size(), cudaMemcpyHostToDevice,
+                                 c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->seg_ptr, seg_ptr.data(), sizeof(long long) * seg_ptr.size(), cudaMemcpyHostToDevice,
                              c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->seg_info, seg_info.data(), sizeof(SegInfo) * seg_info.size(),
@@ -559,6 +592,9 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     A.tasks = reinterpret_cast<const int4*>(c->tasks);
     A.seg_ptr = c->seg_ptr;
     A.seg_info = reinterpret_cast<const int4*>(c->seg_info);
+    A.xtasks = reinterpret_cast<const int4*>(c->xtasks);
+    A.xflux = c->xflux;
+    A.n_xtasks = c->n_xtasks;
     A.ip = c->ip;
     A.is = c->is;
     A.gs = c->gs;
@@ -581,10 +617,13 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     if (flags) A.flags = flags;
     // the adjoint's forward step (branch output) always runs the strict kernel,
     // so its branches are the ones the reverse sweep re-evaluates
-    void* k = (c->arith == SWE_ARITH_FMA && !branch) ? fma_step_kernel(c->params[0].solver)
-                                                     : (void*)kernel_for(c->params[0].solver);
+    const bool fma = c->arith == SWE_ARITH_FMA && !branch;
+    void* k = fma ? fma_step_kernel(c->params[0].solver) : (void*)kernel_for(c->params[0].solver);
+    void* kx = fma ? fma_cross_kernel(c->params[0].solver) : cross_kernel_for(c->params[0].solver);
+    const unsigned xblocks = (unsigned)((c->n_xtasks + 255) / 256);
     void* args[] = {&A};
     for (int64_t s = 0; s < n_steps; ++s) {
+        if (xblocks) CUDA_TRY(cudaLaunchKernel(kx, dim3(xblocks), dim3(256), args, 0, c->stream));
         CUDA_TRY(cudaLaunchKernel(k, dim3(c->grid), dim3(c->block_threads), args, c->smem, c->stream));
         if (!c->capturing) ++c->step_mirror;
     }
@@ -747,6 +786,17 @@ int swe_get_tiling(swe_ctx* c, int32_t* seg_cells, int32_t* block_threads) {
     if (!c) return set_error(SWE_E_INVALID, "null context");
     if (seg_cells) *seg_cells = c->seg_cells;
     if (block_threads) *block_threads = c->block_threads;
+    return SWE_OK;
+}
+
+int swe_get_task_counts(swe_ctx* c, int64_t* n_segments, int64_t* n_tasks, int64_t* n_cross_edges,
+                        int32_t* launches_per_step) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (!c->has_mesh) return set_error(SWE_E_NOMESH, "upload a mesh first");
+    if (n_segments) *n_segments = c->n_seg;
+    if (n_tasks) *n_tasks = c->n_tasks;
+    if (n_cross_edges) *n_cross_edges = c->n_xtasks;
+    if (launches_per_step) *launches_per_step = c->n_xtasks > 0 ? 2 : 1;
     return SWE_OK;
 }
 

@@ -22,6 +22,18 @@ void* fma_step_kernel(int solver) {
     }
 }
 
+void* fma_cross_kernel(int solver) {
+    switch (solver) {
+        case swe_fma::FWAVE: return (void*)swe_fma::cross_edges_kernel<swe_fma::FWAVE>;
+        case swe_fma::AUG_RIEMANN: return (void*)swe_fma::cross_edges_kernel<swe_fma::AUG_RIEMANN>;
+        case swe_fma::LF: return (void*)swe_fma::cross_edges_kernel<swe_fma::LF>;
+        case swe_fma::LF_BATH: return (void*)swe_fma::cross_edges_kernel<swe_fma::LF_BATH>;
+        case swe_fma::LLF: return (void*)swe_fma::cross_edges_kernel<swe_fma::LLF>;
+        case swe_fma::LLF_BATH: return (void*)swe_fma::cross_edges_kernel<swe_fma::LLF_BATH>;
+        default: return nullptr;
+    }
+}
+
 cudaError_t fma_upload_tables() {
     double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
     geometry_tables(leg, vol, nrm);

@@ -192,6 +192,13 @@ class SweContext:
         _lib.check(self.L.swe_get_tiling(self.ptr, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def task_counts(self):
+        """Segments, edge tasks, edges between two segments and kernel launches per step
+        of the uploaded mesh."""
+        s, t, x, k = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int32()
+        _lib.check(self.L.swe_get_task_counts(self.ptr, C.byref(s), C.byref(t), C.byref(x), C.byref(k)))
+        return {"segments": s.value, "tasks": t.value, "cross_edges": x.value, "launches_per_step": k.value}
+
     def upload_mesh(self, mesh):
         ec = np.ascontiguousarray(mesh.edge_cells, np.int64)
         el = np.ascontiguousarray(mesh.edge_local, np.int8)
