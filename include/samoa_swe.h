@@ -162,10 +162,21 @@ int swe_set_staging(swe_ctx* ctx, int32_t depth);
 int swe_set_arith(swe_ctx* ctx, int32_t mode);
 int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads);
 
+/* How the edges between two segments are solved. PASS: once per step by a
+ * kernel before the step kernel, which copies the updates. INKERNEL: by both
+ * segments' CTAs, each keeping its side (no extra launch). AUTO (the default):
+ * PASS for steps on device-resident state (swe_traverse and the calls built on
+ * it), INKERNEL for swe_step_host, whose state is in host memory. The results
+ * are bit identical. No reference counterpart. */
+#define SWE_CROSS_AUTO 0
+#define SWE_CROSS_PASS 1
+#define SWE_CROSS_INKERNEL 2
+int swe_set_cross_pass(swe_ctx* ctx, int32_t mode);
+
 /* Sizes of the uploaded mesh's work lists: segments, edge tasks in the segment
  * lists (an edge between two segments counted once per segment), edges between
  * two segments (computed once per step by a pass before the step kernel) and
- * kernel launches per step (1, or 2 with that pass). Any pointer may be null.
+ * kernel launches per device-resident step (1, or 2 with that pass). Any pointer may be null.
  * No reference counterpart (the reference's sections, src/SFC_edge_traversal.f90). */
 int swe_get_task_counts(swe_ctx* ctx, int64_t* n_segments, int64_t* n_tasks, int64_t* n_cross_edges,
                         int32_t* launches_per_step);

@@ -68,6 +68,7 @@ struct StepArgs {
     int32_t use_tma;
     int32_t fixed_io;          // 1: read h[0], hu[0], hv[0] and write h[1].. on every step (caller's buffers)
     int32_t stage_depth;       // 1: stage a segment, then work on it; 2: stage the next one meanwhile
+    int32_t halo_solve;        // 1: solve the halo tasks here (no cross-edge pass); 0: copy the pass's updates
 };
 
 // Launch bounds of the step kernel: at most 256 threads; with SWE_MIN_BLOCKS
@@ -376,7 +377,7 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         // halo tasks: the cross-edge pass computed these edges' updates; copy
         // this segment's side into its slot
         const long long t0 = A.seg_ptr[seg], t1 = A.seg_ptr[seg + 1];
-        const long long tm = t1 - min((long long)max(si.w, 0), t1 - t0);
+        const long long tm = A.halo_solve ? t1 : t1 - min((long long)max(si.w, 0), t1 - t0);
         for (long long t = tm + tid; t < t1; t += blockDim.x) {
             const int4 tk = __ldg(&A.tasks[t]);
             const uint32_t meta = (uint32_t)tk.z;

@@ -247,6 +247,7 @@ struct swe_ctx {
     int32_t seg_cells = 512, block_threads = 128;  // the best of a sweep on GB300 (2^24 cells)
     int32_t stage_depth = 1;                        // segments staged ahead per CTA (1 or 2)
     int32_t arith = SWE_ARITH_STRICT;
+    int32_t cross_mode = SWE_CROSS_AUTO;
     int64_t n_seg = 0, n_tasks = 0;
     int grid = 0, max_ndepth = 1;
     size_t smem = 0;
@@ -608,6 +609,11 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     A.use_tma = use_tma;
     A.stage_depth = c->stage_depth;
     A.fixed_io = 0;
+    // edges between two segments: a pass before the step kernel for device-resident
+    // steps; solved by both segments' CTAs when the state is in host memory (the
+    // pass's scattered reads of host memory cost more than the duplicated solves)
+    const bool pass = c->n_xtasks > 0 && (c->cross_mode == SWE_CROSS_PASS || (c->cross_mode == SWE_CROSS_AUTO && !io));
+    A.halo_solve = pass ? 0 : 1;
     if (io) {
         A.h[0] = io[0]; A.hu[0] = io[1]; A.hv[0] = io[2];
         A.h[1] = io[3]; A.hu[1] = io[4]; A.hv[1] = io[5];
@@ -620,7 +626,7 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     const bool fma = c->arith == SWE_ARITH_FMA && !branch;
     void* k = fma ? fma_step_kernel(c->params[0].solver) : (void*)kernel_for(c->params[0].solver);
     void* kx = fma ? fma_cross_kernel(c->params[0].solver) : cross_kernel_for(c->params[0].solver);
-    const unsigned xblocks = (unsigned)((c->n_xtasks + 255) / 256);
+    const unsigned xblocks = pass ? (unsigned)((c->n_xtasks + 255) / 256) : 0u;
     void* args[] = {&A};
     for (int64_t s = 0; s < n_steps; ++s) {
         if (xblocks) CUDA_TRY(cudaLaunchKernel(kx, dim3(xblocks), dim3(256), args, 0, c->stream));
@@ -789,6 +795,14 @@ int swe_get_tiling(swe_ctx* c, int32_t* seg_cells, int32_t* block_threads) {
     return SWE_OK;
 }
 
+int swe_set_cross_pass(swe_ctx* c, int32_t mode) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (mode < SWE_CROSS_AUTO || mode > SWE_CROSS_INKERNEL) return set_error(SWE_E_INVALID, "cross mode %d", mode);
+    c->cross_mode = mode;
+    drop_graphs(c);
+    return SWE_OK;
+}
+
 int swe_get_task_counts(swe_ctx* c, int64_t* n_segments, int64_t* n_tasks, int64_t* n_cross_edges,
                         int32_t* launches_per_step) {
     if (!c) return set_error(SWE_E_INVALID, "null context");
@@ -796,7 +810,8 @@ int swe_get_task_counts(swe_ctx* c, int64_t* n_segments, int64_t* n_tasks, int64
     if (n_segments) *n_segments = c->n_seg;
     if (n_tasks) *n_tasks = c->n_tasks;
     if (n_cross_edges) *n_cross_edges = c->n_xtasks;
-    if (launches_per_step) *launches_per_step = c->n_xtasks > 0 ? 2 : 1;
+    if (launches_per_step)
+        *launches_per_step = (c->n_xtasks > 0 && c->cross_mode != SWE_CROSS_INKERNEL) ? 2 : 1;
     return SWE_OK;
 }
 

@@ -192,6 +192,11 @@ class SweContext:
         _lib.check(self.L.swe_get_tiling(self.ptr, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_cross_pass(self, mode):
+        """How edges between two segments are solved: "auto" (default), "pass" (once, by a kernel
+        before the step kernel) or "inkernel" (by both segments' CTAs); bit-identical results."""
+        _lib.check(self.L.swe_set_cross_pass(self.ptr, {"auto": 0, "pass": 1, "inkernel": 2}[mode]))
+
     def task_counts(self):
         """Segments, edge tasks, edges between two segments and kernel launches per step
         of the uploaded mesh."""

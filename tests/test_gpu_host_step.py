@@ -33,8 +33,9 @@ def _resident(scn, steps):
         ctx.close()
 
 
-@pytest.mark.parametrize("where", ["pinned", "device", "device_offset"])
-def test_host_step_matches_resident_step(swe_lib, where):
+@pytest.mark.parametrize("where,cross", [("pinned", "auto"), ("device", "auto"), ("device_offset", "auto"),
+                                         ("pinned", "pass"), ("device", "inkernel")])
+def test_host_step_matches_resident_step(swe_lib, where, cross):
     import torch
     scn = scenarios.radial_dam_break(log2_cells=12, boundary="slip")
     g = scn.grid
@@ -58,6 +59,7 @@ def test_host_step_matches_resident_step(swe_lib, where):
     try:
         ctx.set_params(scn.cfg.params())
         ctx.upload_mesh(g.mesh)
+        ctx.set_cross_pass(cross)
         ctx.set_time(0.0, _dt0(scn))
         for k in range(steps):
             ctx.step_host(*cur, b, *nxt, flags)

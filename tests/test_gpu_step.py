@@ -103,6 +103,31 @@ def test_large_mesh_against_omp(swe_lib, oracle_lib):
         trav.close()
 
 
+@pytest.mark.parametrize("mode", ["pass", "inkernel"])
+def test_cross_segment_modes_against_omp(swe_lib, oracle_lib, mode):
+    """Edges between two segments solved once by the pass before the step kernel,
+    or by both segments' CTAs: the same bits (state, flags, dt) as the oracle."""
+    scn = scenarios.ocean_basin(log2_cells=16, steps=4)
+    g = scn.grid
+    S = omp_state(g.mesh, g)
+    P = oracle_params(scn.cfg)
+    trav = swe.SweEulerTimestepTraversal(scn.cfg)
+    trav.set_tiling(256, 128)
+    trav.ctx.set_cross_pass(mode)
+    try:
+        for k in range(4):
+            S.steps(P, 1)
+            trav.traverse(g)
+            assert_state_equal("%s step %d" % (mode, k), g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+            assert np.array_equal(g.refinement, S.flags)
+            assert g.r_dt == S.scal[1] and g.r_time == S.scal[0]
+        counts = trav.ctx.task_counts()
+        assert counts["segments"] == g.mesh.n_cells // 256 and counts["cross_edges"] > 0
+        assert counts["launches_per_step"] == (2 if mode == "pass" else 1)
+    finally:
+        trav.close()
+
+
 def _odd_mesh(depth):
     """A uniform mesh with its last cell removed: odd cell count, the removed
     cell's neighbours get boundary edges instead. Exercises ragged segments."""
@@ -120,14 +145,15 @@ def _odd_mesh(depth):
 
 
 def test_full_size_basin_against_omp(swe_lib, oracle_lib):
-    """The bench workload itself, 2^26 cells with the autotuned tiling (768 x 256):
-    three steps bit-exact against the OpenMP oracle, state, flags, dt."""
+    """The bench workload itself, 2^26 cells with the autotuned tiling (512 x 128)
+    and the cross-edge pass: three steps bit-exact against the OpenMP oracle,
+    state, flags, dt."""
     scn = scenarios.ocean_basin(log2_cells=26, steps=3, device="cuda")
     g = scn.grid
     S = omp_state(g.mesh, g)
     P = oracle_params(scn.cfg)
     trav = swe.SweEulerTimestepTraversal(scn.cfg)
-    trav.set_tiling(768, 256)
+    trav.set_tiling(512, 128)
     try:
         for k in range(3):
             S.steps(P, 1)
