@@ -348,6 +348,7 @@ def adjoint_compare(a, device):
         # differences straddle it
         deep = case["b"] < -100.0
         errs = {"h0": [], "b": []}
+        nerr = []  # |fd - ad| / (|g| |d|): the error against the directional scale of the gradient
         for key, n_dir in (("h0", a.adjoint_fd), ("b", max(1, a.adjoint_fd // 4) if a.adjoint_fd else 0)):
             for k in range(n_dir):
                 d = rng.normal(size=gh.shape) * deep
@@ -362,6 +363,8 @@ def adjoint_compare(a, device):
                     Jm = P.objective(case["h0"], case["b"] - eps * d, record=False)
                     ad = float(gb @ d)
                 errs[key].append(abs((Jp - Jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
+                if key == "h0":
+                    nerr.append(abs((Jp - Jm) / (2 * eps) - ad) / max(np.linalg.norm(gh) * np.linalg.norm(d), 1e-300))
         t_step, t_adj = adjoint.time_steps(P, case["h0"], case["b"], 50)
     finally:
         P.close()
@@ -371,11 +374,17 @@ def adjoint_compare(a, device):
             "adjoint_steps": stats["adjoint_steps"], "fd_directions_h0": len(errs["h0"]),
             "fd_max_rel_err_h0": max(errs["h0"], default=None),
             "fd_median_rel_err_h0": float(np.median(errs["h0"])) if errs["h0"] else None,
+            "fd_directions_h0_within_1e-6": int(sum(e <= 1e-6 for e in errs["h0"])),
+            "fd_max_err_over_grad_norm_h0": max(nerr, default=None),
             "fd_directions_b": len(errs["b"]), "fd_max_rel_err_b_unfrozen": max(errs["b"], default=None),
             "forward_step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj, "adjoint_step_over_forward_step": t_adj / t_step,
             "note": "gradient_s = one checkpointed sweep (its first descent is the forward run; recomputation "
                     "included); J(h0, b) is the squared misfit at 32 gauges; dt frozen, FD with the same dts, "
-                    "eps = 1e-6 relative, seeded N(0,1) directions on the cells deeper than 100 m; perturbing b "
+                    "eps = 1e-6 relative, seeded N(0,1) directions on the cells deeper than 100 m. J is piecewise "
+                    "smooth: in the nearly still basin the f-wave's middle wave speed 0.5 (s1 + s2) sits near 0, and "
+                    "its sign sends the shear wave to the left or the right cell, so perturbations flip branches and "
+                    "J jumps slightly; the per-direction error is branch-limited (measured: not monotone in eps, "
+                    "no better with a 4-point stencil), the error against |g| |d| stays small; perturbing b "
                     "reorders neighbouring depths at rest and so crosses the Einfeldt min/max kinks over 2,000 "
                     "steps, so plain FD in b is kink-limited (the branch-frozen FD check of b is in the tests)"}
 

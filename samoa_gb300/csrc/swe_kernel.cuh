@@ -369,8 +369,14 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         double* sh_hv = sh_hu + T;
         double* sh_b = sh_hv + T;
         for (int i = tid; i < cn; i += blockDim.x) {
-            double d, sq, y;
-            depth_terms(State{sh_h[i], 0.0, 0.0, sh_b[i]}, P.drytol, d, sq, y);
+            // depth_terms, with the square root and reciprocal skipped by warps of dry cells
+            const double d = sh_h[i] - sh_b[i];
+            const bool wet = lt(P.drytol, d);
+            double sq = 0.0, y = 0.0;
+            if (__any_sync(__activemask(), wet)) {
+                sq = wet ? sqrt(kG * d) : 0.0;
+                y = wet ? recip_rn(d).y : 0.0;
+            }
             sh_rh[i] = y;
             sh_sq[i] = sq;
         }
@@ -472,14 +478,33 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             const int d = A.depth[c];
             const int di = d - P.dmin;
             const double leg = tab_leg[di], hyp = tab_hyp[di], ndv = tab_ndv[di];
-            double dh = z0(imul_cell(leg, upd[(0 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(0 * 3 + 1) * T + i]);
-            dh = dh + imul_cell(leg, upd[(0 * 3 + k2) * T + i]);
-            double dp1 = z0(imul_cell(leg, upd[(1 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(1 * 3 + 1) * T + i]);
-            dp1 = dp1 + imul_cell(leg, upd[(1 * 3 + k2) * T + i]);
-            double dp2 = z0(imul_cell(leg, upd[(2 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(2 * 3 + 1) * T + i]);
-            dp2 = dp2 + imul_cell(leg, upd[(2 * 3 + k2) * T + i]);
-            double ds = z0(imul_cell(leg, upd[(3 * 3 + k0) * T + i])) + imul_cell(hyp, upd[(3 * 3 + 1) * T + i]);
-            ds = ds + imul_cell(leg, upd[(3 * 3 + k2) * T + i]);
+            double u[4][3];
+            long long nz = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                u[q][0] = upd[(q * 3 + k0) * T + i];
+                u[q][1] = upd[(q * 3 + 1) * T + i];
+                u[q][2] = upd[(q * 3 + k2) * T + i];
+                nz |= (dbits(u[q][0]) | dbits(u[q][1]) | dbits(u[q][2])) << 1;
+            }
+            // quiet: every edge update is +-0 (dry land, water at rest). Then each sum
+            // below is +0 (positive edge lengths), RN(ndv * +0) is a zero with ndv's sign,
+            // and adding it leaves the state as add_zero says: the same bits, without
+            // the FP64 arithmetic.
+            const bool quiet = nz == 0 && is_finite(ndv);
+            double dh = 0.0, dp1 = 0.0, dp2 = 0.0, ds = 0.0;
+            if (__any_sync(__activemask(), !quiet)) {
+                if (!quiet) {
+                    dh = z0(imul_cell(leg, u[0][0])) + imul_cell(hyp, u[0][1]);
+                    dh = dh + imul_cell(leg, u[0][2]);
+                    dp1 = z0(imul_cell(leg, u[1][0])) + imul_cell(hyp, u[1][1]);
+                    dp1 = dp1 + imul_cell(leg, u[1][2]);
+                    dp2 = z0(imul_cell(leg, u[2][0])) + imul_cell(hyp, u[2][1]);
+                    dp2 = dp2 + imul_cell(leg, u[2][2]);
+                    ds = z0(imul_cell(leg, u[3][0])) + imul_cell(hyp, u[3][1]);
+                    ds = ds + imul_cell(leg, u[3][2]);
+                }
+            }
             int8_t f = 0;
             // |dh| > thr and |dh| < thr / 8 on the bit patterns (thresholds are positive;
             // a NaN |dh| passes neither test, as in IEEE)
@@ -496,9 +521,13 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             } else {
                 dtmin = dmn(dtmin, tab_vol[di] / ds);
             }
-            dh = imul_cell(ndv, dh);
-            dp1 = imul_cell(ndv, dp1);
-            dp2 = imul_cell(ndv, dp2);
+            if (quiet) {
+                dh = dp1 = dp2 = bitsd(dbits(ndv) & (long long)0x8000000000000000ULL);  // RN(ndv * +0)
+            } else {
+                dh = imul_cell(ndv, dh);
+                dp1 = imul_cell(ndv, dp1);
+                dp2 = imul_cell(ndv, dp2);
+            }
             double h = sh_h[i], p1 = sh_hu[i], p2 = sh_hv[i];
             const double b = sh_b[i];
             uint8_t br = 0;
@@ -509,9 +538,15 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
                 p2 = 0.0;
                 br = 1;
             }
-            h = h + dh;
-            p1 = p1 + dp1;
-            p2 = p2 + dp2;
+            if (quiet) {
+                h = add_zero(h, dh);
+                p1 = add_zero(p1, dp1);
+                p2 = add_zero(p2, dp2);
+            } else {
+                h = h + dh;
+                p1 = p1 + dp1;
+                p2 = p2 + dp2;
+            }
             if (lt(h, bdry)) {  // dried out: surface to min(b, 0), at rest
                 h = lt0(b) ? b : 0.0;
                 p1 = 0.0;

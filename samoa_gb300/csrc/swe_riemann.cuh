@@ -151,6 +151,18 @@ __device__ __forceinline__ double mul_here(double a, double b) {
     asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
     return r;
 }
+// x + z for z = +-0, as IEEE addition gives it: x itself, except that a zero x
+// takes +0 unless both are -0; a NaN x takes the FP64 add.
+__device__ __forceinline__ double add_zero(double x, double z) {
+    const long long b = dbits(x);
+    if ((b << 1) == 0) return bitsd(b & dbits(z));  // -0 only when both are -0
+    if (abs_bits(x) > 0x7ff0000000000000LL) {
+        double r;
+        asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(x), "d"(z));
+        return r;
+    }
+    return x;
+}
 // RN(x * p) for p = 2^k: while x and the result are normal numbers the product
 // is exact and only the exponent field moves (an integer add on the bit
 // pattern); +-0 stays itself; a subnormal, infinite or NaN operand and an
@@ -523,6 +535,13 @@ template <int SOLVER>
 __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR, double dL,
                                              double dR, double sqL, double sqR, double yL, double yR,
                                              double drytol, Update& fL, Update& fR, int axis = 0) {
+    // both sides dry: the solver returns zero net updates and speed, and their
+    // rotation back is +0 in every component, so neither rotation is needed
+    if (!lt(drytol, dL) && !lt(drytol, dR) && !is_nan(dL) && !is_nan(dR) && !is_nan(drytol)) {
+        fL = Update{0.0, 0.0, 0.0, 0.0};
+        fR = Update{0.0, 0.0, 0.0, 0.0};
+        return;
+    }
     const bool fin = is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
     const bool fast = axis != 0 && fin;
     const bool diag = axis == 0 && fin && abs_bits(n1) == abs_bits(n2);
