@@ -193,7 +193,9 @@ int swe_mesh_uniform_vertices(int32_t depth, double* vertices);
  * bisections) gives the plotter types, the edge streams in the swe_mesh_upload
  * layout, and optionally centroids[2n] and vertices[6n]. With plotter_out and
  * the edge arrays NULL only the counts *n_edges, *n_bnd are returned (sizes:
- * edge_cells, edge_local 2 * n_edges; bnd_cell, bnd_local n_bnd).
+ * edge_cells, edge_local 2 * n_edges; bnd_cell, bnd_local n_bnd). Since every
+ * cell has three edges, 2 * n_edges + n_bnd = 3 * n_cells: arrays of 3 * n_cells
+ * entries each always suffice, and one call with them returns counts and streams.
  * SWE_E_INVALID if the depths are not the leaves of such a tree or the tree is
  * not conforming. The host side of the remesh handoff. */
 int swe_mesh_build(int64_t n_cells, const int8_t* depth, int64_t* n_edges, int64_t* n_bnd, int8_t* plotter_out,

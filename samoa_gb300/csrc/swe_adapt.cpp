@@ -24,35 +24,10 @@
 
 namespace swe {
 
-namespace {
-
-// Which local edge (0..2) of a cell is its leg (x0, x1), where x0 -> x2 is the
-// hypotenuse and x1 the right-angle vertex of the walk's vertex order: the
-// outward normal of (x0, x1) points along x1 - x2, so its dot product with
-// x2 - x0 is negative, the other leg's positive. (Which end of the hypotenuse
-// comes first is not a function of the plotter type alone, so it is decided
-// per cell from its vertices.)
-struct LegTable {
-    double normal[17][3][2];
-    LegTable() {
-        double leg[kMaxDepth + 2], vol[kMaxDepth + 1];
-        geometry_tables(leg, vol, normal);
-    }
-};
-
-int leg_a_local(const LegTable& t, int plotter, const double* x) {
-    const double* n = t.normal[plotter + 8][0];
-    const double d = n[0] * (x[4] - x[0]) + n[1] * (x[5] - x[1]);
-    return d < 0.0 ? 0 : 2;
-}
-
-}  // namespace
-
 int mesh_adapt(int64_t n, const int8_t* depth, const int8_t* flags, const double* const in[4], AdaptResult& out) {
     if (n < 2 || !depth || !flags) return set_error(SWE_E_INVALID, "bad mesh or flags");
-    static const LegTable legs;
     BuiltMesh m;
-    int rc = build_mesh(n, depth, 0, true, m);
+    int rc = build_mesh(n, depth, 0, kWantLegs, m);
     if (rc) return rc;
     const int64_t ne = m.ne, nb = m.nb;
     // edge ids: inner edges 0..ne-1, boundary edges ne..ne+nb-1
@@ -63,7 +38,7 @@ int mesh_adapt(int64_t n, const int8_t* depth, const int8_t* flags, const double
     // per cell: hypotenuse, leg (x0, x1) = the first child's hypotenuse, leg (x1, x2)
     std::vector<int64_t> eh((size_t)n), ea((size_t)n), eb((size_t)n);
     for (int64_t k = 0; k < n; ++k) {
-        const int la = leg_a_local(legs, m.plotter[(size_t)k], &m.vert[(size_t)(6 * k)]);
+        const int la = m.leg[(size_t)k];  // local index of the leg (x0, x1)
         eh[(size_t)k] = slot[(size_t)(3 * k + 1)];
         ea[(size_t)k] = slot[(size_t)(3 * k + la)];
         eb[(size_t)k] = slot[(size_t)(3 * k + 2 - la)];
@@ -154,7 +129,7 @@ int swe_mesh_build(int64_t n_cells, const int8_t* depth, int64_t* n_edges, int64
     if (any && (!plotter_out || !edge_cells || !edge_local || !bnd_cell || !bnd_local))
         return set_error(SWE_E_INVALID, "mesh outputs must all be given (centroids, vertices optional)");
     BuiltMesh m;
-    int rc = build_mesh(n_cells, depth, 0, centroids || vertices, m);
+    int rc = build_mesh(n_cells, depth, 0, (centroids || vertices) ? kWantVertices : 0, m);
     if (rc) return rc;
     if (n_edges) *n_edges = m.ne;
     if (n_bnd) *n_bnd = m.nb;

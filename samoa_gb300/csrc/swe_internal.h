@@ -84,8 +84,12 @@ struct BuiltMesh {
     std::vector<int8_t> depth, plotter, el, bl;
     std::vector<int64_t> ec, bc;
     std::vector<double> vert;     // 6 per cell (optional)
+    std::vector<int8_t> leg;      // per cell (optional): the local edge index of the leg (x0, x1)
     std::vector<int64_t> parent;  // the bisected node a leaf came from (negative for the two roots)
 };
+// What build_mesh records besides the streams.
+constexpr int kWantVertices = 1;  // BuiltMesh::vert
+constexpr int kWantLegs = 2;      // BuiltMesh::leg
 // Result of one remesh (swe_adapt.cpp): new leaf depths in traversal order, for
 // each new cell its source cell(s) (second = -1 unless two siblings merged),
 // and the transferred h, hu, hv, b (empty where no input was given).
@@ -100,7 +104,7 @@ struct AdaptResult {
     }
 };
 int mesh_adapt(int64_t n, const int8_t* depth, const int8_t* flags, const double* const in[4], AdaptResult& out);
-int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, bool want_vertices, BuiltMesh& m);
+int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, int want, BuiltMesh& m);
 int export_mesh(const BuiltMesh& m, int8_t* depth_out, int8_t* plotter_out, int64_t* edge_cells, int8_t* edge_local,
                 int64_t* bnd_cell, int8_t* bnd_local, double* centroids, double* vertices);
 int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, int8_t* depth_out,

@@ -72,7 +72,20 @@ int64_t uniform_boundary_edges(int depth) { return (int64_t)4 << (depth / 2); }
 // bisected while it is shallower than the next leaf's depth), numbering the
 // edges the way the traversal's colour-edge stacks meet them. A uniform mesh
 // is the sequence of 2^(d+1) leaves of depth d.
-int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, bool want_vertices, BuiltMesh& m) {
+namespace {
+// Outward unit normals of the local edges by plotter type (geometry_tables).
+struct NormalTable {
+    double n[17][3][2];
+    NormalTable() {
+        double leg[kMaxDepth + 2], vol[kMaxDepth + 1];
+        geometry_tables(leg, vol, n);
+    }
+};
+}  // namespace
+
+int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, int want, BuiltMesh& m) {
+    const bool want_vertices = (want & kWantVertices) != 0, want_legs = (want & kWantLegs) != 0;
+    static const NormalTable normals;
     const bool uniform = leaf_depth == nullptr;
     if (uniform) n_leaves = (int64_t)2 << uniform_depth;
     if (n_leaves < 2) return set_error(SWE_E_INVALID, "a mesh has at least the two root cells");
@@ -86,6 +99,8 @@ int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, bo
     m.bl.clear();
     if (want_vertices) m.vert.assign((size_t)(6 * n_leaves), 0.0);
     else m.vert.clear();
+    if (want_legs) m.leg.assign((size_t)n_leaves, 0);
+    else m.leg.clear();
 
     struct Item {
         GrammarCell c;
@@ -138,6 +153,16 @@ int build_mesh(int64_t n_leaves, const int8_t* leaf_depth, int uniform_depth, bo
                 m.vert[(size_t)(6 * k + 2 * v)] = it.x[v][0];
                 m.vert[(size_t)(6 * k + 2 * v + 1)] = it.x[v][1];
             }
+        if (want_legs) {
+            // which local edge is the leg (x0, x1), where x0 -> x2 is the hypotenuse and
+            // x1 the right-angle vertex: the outward normal of (x0, x1) points along
+            // x1 - x2, so its dot product with x2 - x0 is negative, the other leg's
+            // positive (which end of the hypotenuse comes first is not a function of
+            // the plotter type alone)
+            const double* nv = normals.n[c.plotter + 8][0];
+            const double dd = nv[0] * (it.x[2][0] - it.x[0][0]) + nv[1] * (it.x[2][1] - it.x[0][1]);
+            m.leg[(size_t)k] = dd < 0.0 ? 0 : 2;
+        }
         const int8_t ip = kPrevIdx[c.turtle], ic = kColorIdx[c.turtle], in = kNextIdx[c.turtle];
         // previous crossed edge: the open crossed edge of the previous cell, or the boundary
         if (!c.prev_bnd) {
@@ -208,7 +233,7 @@ int mesh_uniform(int depth, int64_t* n_cells, int64_t* n_edges, int64_t* n_bnd, 
     if (!depth_out || !plotter_out || !edge_cells || !edge_local || !bnd_cell || !bnd_local)
         return set_error(SWE_E_INVALID, "mesh outputs must all be given (centroids optional)");
     BuiltMesh m;
-    int rc = build_mesh(n, nullptr, depth, centroids || vertices, m);
+    int rc = build_mesh(n, nullptr, depth, (centroids || vertices) ? kWantVertices : 0, m);
     if (rc) return rc;
     return export_mesh(m, depth_out, plotter_out, edge_cells, edge_local, bnd_cell, bnd_local, centroids, vertices);
 }

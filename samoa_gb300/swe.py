@@ -89,18 +89,20 @@ def mesh_from_depths(depths, centroids=True, vertices=False):
     L = _lib.load()
     d = np.ascontiguousarray(depths, np.int8)
     n = len(d)
+    # 2 * n_edges + n_bnd = 3 * n: arrays of that bound take one walk (the
+    # untouched tails are never paged in)
     ne, nb = C.c_int64(), C.c_int64()
-    _lib.check(L.swe_mesh_build(n, _p(d), C.byref(ne), C.byref(nb), *([None] * 7)))
-    ne, nb = ne.value, nb.value
     p = np.empty(n, np.int8)
-    ec = np.empty((ne, 2), np.int64)
-    el = np.empty((ne, 2), np.int8)
-    bc = np.empty(nb, np.int64)
-    bl = np.empty(nb, np.int8)
+    ec = np.empty(((3 * n) // 2, 2), np.int64)
+    el = np.empty(((3 * n) // 2, 2), np.int8)
+    bc = np.empty(3 * n, np.int64)
+    bl = np.empty(3 * n, np.int8)
     cen = np.empty((n, 2), np.float64) if centroids else None
     ver = np.empty((n, 3, 2), np.float64) if vertices else None
-    _lib.check(L.swe_mesh_build(n, _p(d), None, None, _p(p), _p(ec), _p(el), _p(bc), _p(bl), _p(cen), _p(ver)))
-    return Mesh(d.copy(), p, ec, el, bc, bl, cen, vertices=ver)
+    _lib.check(L.swe_mesh_build(n, _p(d), C.byref(ne), C.byref(nb), _p(p), _p(ec), _p(el), _p(bc), _p(bl), _p(cen),
+                                _p(ver)))
+    ne, nb = ne.value, nb.value
+    return Mesh(d.copy(), p, ec[:ne], el[:ne], bc[:nb].copy(), bl[:nb].copy(), cen, vertices=ver)
 
 
 def adapt(mesh, flags, h=None, hu=None, hv=None, b=None, with_source=False):
