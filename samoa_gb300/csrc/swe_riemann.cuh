@@ -251,55 +251,86 @@ __device__ __forceinline__ double div_rn(double a, const Recip& r) {
 }
 
 
+// Non-strict comparisons on the integer pipe with IEEE semantics (false if either is NaN).
+__device__ __forceinline__ bool le(double a, double b) {  // a <= b
+    return !is_nan(a) && !is_nan(b) && ord_key(a) <= ord_key(b);
+}
+__device__ __forceinline__ double iabs(double x) { return bitsd(abs_bits(x)); }  // fabs
+
+// RN(1 / h) from a precomputed reciprocal y when it is known to be correctly
+// rounded (recip_rn's fast range), else the IEEE division.
+__device__ __forceinline__ double inv_of(double h, double y, bool y_ok) { return y_ok ? y : 1.0 / h; }
+
 // Riemann structure with one Newton step, src/geoclaw/riemannsolvers.f:507-618.
-static __device__ __noinline__ void riemann_structure(double hL, double hR, double uL, double uR, double drytol,
-                                               double& hm, double& s1m, double& s2m) {
+// sqL / sqR are sqrt(g * hL) and sqrt(g * hR) (the caller's, the same operands
+// and so the same bits as computing them here); yL / yR are RN(1 / hL) and
+// RN(1 / hR) where yL_ok / yR_ok, else the divisions are done here.
+__device__ __forceinline__ void riemann_structure_core(double hL, double hR, double uL, double uR, double drytol,
+                                                      double sqL, double sqR, double yL, double yR, bool yL_ok,
+                                                      bool yR_ok, double& hm, double& s1m, double& s2m) {
     const double g = kG;
-    double h_min = dmn(hR, hL);
-    double h_max = dmx(hR, hL);
+    const bool r_lower = lt(hR, hL);  // h_min = dmn(hR, hL) is hR
+    const double h_min = r_lower ? hR : hL, sq_min = r_lower ? sqR : sqL;
+    const bool r_higher = lt(hL, hR);  // h_max = dmx(hR, hL) is hR
+    const double h_max = r_higher ? hR : hL, sq_max = r_higher ? sqR : sqL;
     double delu = uR - uL;
-    if (h_min <= drytol) {
+    if (le(h_min, drytol)) {
         hm = 0.0;
-        double t = ((uR + uL) - 2.0 * sqrt(g * hR)) + 2.0 * sqrt(g * hL);
+        double t = ((uR + uL) - scale_pow2(sqR, 1, 2.0)) + scale_pow2(sqL, 1, 2.0);
         s1m = t;
         s2m = t;
         return;
     }
-    double F_min = delu + 2.0 * (sqrt(g * h_min) - sqrt(g * h_max));
+    double F_min = delu + scale_pow2(sq_min - sq_max, 1, 2.0);
     double F_max = delu + (h_max - h_min) * sqrt(((0.5 * g) * (h_max + h_min)) / (h_max * h_min));
-    if (F_min > 0.0) {  // two rarefactions
-        double t = dmx(0.0, -delu + 2.0 * (sqrt(g * hL) + sqrt(g * hR)));
+    if (gt0(F_min)) {  // two rarefactions
+        double t = imax(0.0, -delu + scale_pow2(sqL + sqR, 1, 2.0));
         hm = (1.0 / (16.0 * g)) * (t * t);
-        s1m = (uL + 2.0 * sqrt(g * hL)) - 3.0 * sqrt(g * hm);
-        s2m = (uR - 2.0 * sqrt(g * hR)) + 3.0 * sqrt(g * hm);
-    } else if (F_max <= 0.0) {  // two shocks: one Newton step on sqrt(h)
+        const double sqm = sqrt(g * hm);
+        s1m = (uL + scale_pow2(sqL, 1, 2.0)) - 3.0 * sqm;
+        s2m = (uR - scale_pow2(sqR, 1, 2.0)) + 3.0 * sqm;
+    } else if (le(F_max, 0.0)) {  // two shocks: one Newton step on sqrt(h)
         double h0 = h_max;
-        double gL = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hL));
-        double gR = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hR));
+        const double i0 = r_higher ? inv_of(hR, yR, yR_ok) : inv_of(hL, yL, yL_ok);
+        const double iL = inv_of(hL, yL, yL_ok), iR = inv_of(hR, yR, yR_ok);
+        double gL = sqrt((0.5 * g) * (i0 + iL));
+        double gR = sqrt((0.5 * g) * (i0 + iR));
         double F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR;
         double dfdh = ((gL - (g * (h0 - hL)) / ((4.0 * (h0 * h0)) * gL)) + gR) -
                       (g * (h0 - hR)) / ((4.0 * (h0 * h0)) * gR);
-        double slope = (2.0 * sqrt(h0)) * dfdh;
-        double t = sqrt(h0) - F0 / slope;
+        const double sq0 = sqrt(h0);
+        double slope = scale_pow2(sq0, 1, 2.0) * dfdh;
+        double t = sq0 - F0 / slope;
         hm = t * t;
-        double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hL));
-        double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hR));
-        s1m = u1m - sqrt(g * hm);
-        s2m = u2m + sqrt(g * hm);
+        const double im = 1.0 / hm;
+        double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (im + iL));
+        double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (im + iR));
+        const double sqm = sqrt(g * hm);
+        s1m = u1m - sqm;
+        s2m = u2m + sqm;
     } else {  // one shock, one rarefaction
         double h0 = h_min;
-        double F0 = (delu + 2.0 * (sqrt(g * h0) - sqrt(g * h_max))) +
-                    (h0 - h_min) * sqrt((0.5 * g) * (1.0 / h0 + 1.0 / h_min));
+        const double i0 = r_lower ? inv_of(hR, yR, yR_ok) : inv_of(hL, yL, yL_ok);
+        double F0 = (delu + scale_pow2(sq_min - sq_max, 1, 2.0)) + (h0 - h_min) * sqrt((0.5 * g) * (i0 + i0));
         double slope = (F_max - F0) / (h_max - h_min);
         hm = h0 - F0 / slope;
-        if (hL > hR) {
-            s1m = (uL + 2.0 * sqrt(g * hL)) - 3.0 * sqrt(g * hm);
-            s2m = (uL + 2.0 * sqrt(g * hL)) - sqrt(g * hm);
+        const double sqm = sqrt(g * hm);
+        if (lt(hR, hL)) {
+            s1m = (uL + scale_pow2(sqL, 1, 2.0)) - 3.0 * sqm;
+            s2m = (uL + scale_pow2(sqL, 1, 2.0)) - sqm;
         } else {
-            s2m = (uR - 2.0 * sqrt(g * hR)) + 3.0 * sqrt(g * hm);
-            s1m = (uR - 2.0 * sqrt(g * hR)) + sqrt(g * hm);
+            s2m = (uR - scale_pow2(sqR, 1, 2.0)) + 3.0 * sqm;
+            s1m = (uR - scale_pow2(sqR, 1, 2.0)) + sqm;
         }
     }
+}
+
+// The same with sqrt(g * h) and the reciprocals computed here (the wet/dry
+// edges' wall test; a call, so the callers keep their registers).
+static __device__ __noinline__ void riemann_structure(double hL, double hR, double uL, double uR, double drytol,
+                                                      double& hm, double& s1m, double& s2m) {
+    riemann_structure_core(hL, hR, uL, uR, drytol, sqrt(kG * hL), sqrt(kG * hR), 0.0, 0.0, false, false, hm, s1m,
+                           s2m);
 }
 
 __device__ __forceinline__ double det3(double a00, double a01, double a02, double a10, double a11, double a12,
@@ -310,75 +341,120 @@ __device__ __forceinline__ double det3(double a00, double a01, double a02, doubl
     return (d1 - d2) + d3;
 }
 
+// RN(0 * x): a zero with x's sign for finite x (0 * inf and 0 * NaN are NaN).
+__device__ __forceinline__ double mul0(double x) {
+    return is_finite(x) ? bitsd(dbits(x) & (long long)0x8000000000000000ULL) : x * 0.0;
+}
+// |x| < 2^300 (or zero): products of three such numbers neither overflow nor are infinite
+__device__ __forceinline__ bool moderate(double x) { return abs_bits(x) < 0x52b0000000000000LL; }
+
 // Augmented solver (George 2008) with maxiter = 1, src/geoclaw/riemannsolvers.f:2-258.
 // The entropy corrector is off in the source; with one iteration the star
 // states after the Cramer solve never reach the outputs.
+// sqL / sqR: sqrt(g * h) of the (fixed-up) depths; yL / yR: RN(1 / h) where yL_ok / yR_ok.
+//
+// The 3x3 Cramer solve has the eigenvector matrix R = [[1, 0, 1], [l0, 0, l2],
+// [l0^2, 1, l2^2]] with constant 0 and 1 entries. Evaluated in the source's
+// order, a product by 1 is its other factor and a product by 0 a signed zero,
+// and subtracting or adding a zero leaves a nonzero value unchanged, so for
+// finite operands the four determinants have the values
+//   det(R) = RN(l0 - l2), the numerators RN(e1 - RN(e0 l2)), the full
+//   expression for beta1, and RN(RN(e0 l0) - e1)
+// with at most a different sign of a zero result. Such a zero only reaches the
+// f-waves, whose zeros the net-update accumulation turns into +0, except as a
+// divisor: a zero determinant, and operands that are not finite or so large
+// that a product could overflow, take the source's full expressions.
 static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
-                                         double uL, double uR, double vL, double vR, double delphi, double sE1,
-                                         double sE2, double sqL, double sqR, double drytol, double sw[3],
-                                         double fw[3][3]) {
+                                                double uL, double uR, double vL, double vR, double delphi,
+                                                double sE1, double sE2, double sqL, double sqR, double yL,
+                                                double yR, bool yL_ok, bool yR_ok, double drytol, double sw[3],
+                                                double fw[3][3]) {
     const double g = kG;
     double delh = hR - hL;
     double delhu = huR - huL;
     double delb = bR - bL;
     double hm, s1m, s2m;
-    riemann_structure(hL, hR, uL, uR, drytol, hm, s1m, s2m);
-    double l0 = dmn(sE1, s2m);
-    double l2 = dmx(sE2, s1m);
+    riemann_structure_core(hL, hR, uL, uR, drytol, sqL, sqR, yL, yR, yL_ok, yR_ok, hm, s1m, s2m);
+    double l0 = imin(sE1, s2m);
+    double l2 = imax(sE2, s1m);
     sE1 = l0;
     sE2 = l2;
-    double hstarHLL = dmx((((huL - huR) + sE2 * hR) - sE1 * hL) / (sE2 - sE1), 0.0);
-    double l1 = 0.5 * (l0 + l2);
-    if (fabs(l1) < 1e-20) l1 = 0.0;
-    // eigenvectors: columns (1, l, l^2) for waves 1 and 3, (0, 0, 1) for wave 2
-    const double r00 = 1.0, r01 = 0.0, r02 = 1.0;
-    const double r10 = l0, r11 = 0.0, r12 = l2;
-    const double r20 = l0 * l0, r21 = 1.0, r22 = l2 * l2;
+    // sE2 - sE1 = -(l0 - l2) exactly (round to nearest is symmetric): one
+    // reciprocal serves hstarHLL's divisor and the Cramer determinant
+    const double dsp = sE2 - sE1;
+    const Recip rsp = recip_rn(dsp);
+    double hstarHLL = imax(div_rn(((huL - huR) + sE2 * hR) - sE1 * hL, rsp), 0.0);
+    double l1 = scale_pow2(l0 + l2, -1, 0.5);
+    if (lt(iabs(l1), 1e-20)) l1 = 0.0;
+    const double r20 = l0 * l0, r22 = l2 * l2;
 
     const double ct = 1e-6;
-    double hbar = dmx(0.5 * (hL + hR), 0.0);
+    double hbar = imax(scale_pow2(hL + hR, -1, 0.5), 0.0);
     double su = uL + uR;
-    double s1s2bar = 0.25 * (su * su) - g * hbar;
-    double s1s2tilde = dmx(0.0, uL * uR) - g * hbar;
-    bool sonic = false;
-    if (fabs(s1s2bar) <= ct) sonic = true;
-    if (s1s2bar * s1s2tilde <= ct) sonic = true;
-    if ((s1s2bar * sE1) * sE2 <= ct) sonic = true;
-    if (dmn(fabs(sE1), fabs(sE2)) < ct) sonic = true;
-    if (sE1 < 0.0 && s1m > 0.0) sonic = true;
-    if (sE2 > 0.0 && s2m < 0.0) sonic = true;
-    if ((uL + sqL) * (uR + sqR) < 0.0) sonic = true;  // sqrt(g * h) of the fixed-up depths
-    if ((uL - sqL) * (uR - sqR) < 0.0) sonic = true;
+    const double ghbar = g * hbar;
+    double s1s2bar = scale_pow2(su * su, -2, 0.25) - ghbar;
+    double s1s2tilde = imax(0.0, uL * uR) - ghbar;
+    bool sonic = le(iabs(s1s2bar), ct);
+    sonic |= le(s1s2bar * s1s2tilde, ct);
+    sonic |= le((s1s2bar * sE1) * sE2, ct);
+    sonic |= lt(imin(iabs(sE1), iabs(sE2)), ct);
+    sonic |= lt0(sE1) && gt0(s1m);
+    sonic |= gt0(sE2) && lt0(s2m);
+    sonic |= lt0((uL + sqL) * (uR + sqR));  // sqrt(g * h) of the fixed-up depths
+    sonic |= lt0((uL - sqL) * (uR - sqR));
 
-    double deldelh = sonic ? -delb : ((delb * g) * hbar) / s1s2bar;
-    if (sE1 < -ct && sE2 > ct) {
-        deldelh = dmn(deldelh, (hstarHLL * (sE2 - sE1)) / sE2);
-        deldelh = dmx(deldelh, (hstarHLL * (sE2 - sE1)) / sE1);
-    } else if (sE1 >= ct) {
-        deldelh = dmn(deldelh, (hstarHLL * (sE2 - sE1)) / sE1);
-        deldelh = dmx(deldelh, -hL);
-    } else if (sE2 <= -ct) {
-        deldelh = dmn(deldelh, hR);
-        deldelh = dmx(deldelh, (hstarHLL * (sE2 - sE1)) / sE2);
+    double deldelh, deldelphi;
+    const double dgh = (delb * g) * hbar;
+    if (sonic) {
+        deldelh = flip(delb, true);
+        deldelphi = flip(ghbar * delb, true);
+    } else {
+        const Recip rb = recip_rn(s1s2bar);
+        deldelh = div_rn(dgh, rb);
+        deldelphi = flip(div_rn(dgh * s1s2tilde, rb), true);
     }
-    double deldelphi = sonic ? -((g * hbar) * delb) : -((((delb * g) * hbar) * s1s2tilde) / s1s2bar);
-    deldelphi = dmn(deldelphi, g * dmx(-(hL * delb), -(hR * delb)));
-    deldelphi = dmx(deldelphi, g * dmn(-(hL * delb), -(hR * delb)));
+    const double hsd = hstarHLL * dsp;
+    if (lt(sE1, -ct) && lt(ct, sE2)) {
+        deldelh = imin(deldelh, hsd / sE2);
+        deldelh = imax(deldelh, hsd / sE1);
+    } else if (le(ct, sE1)) {
+        deldelh = imin(deldelh, hsd / sE1);
+        deldelh = imax(deldelh, flip(hL, true));
+    } else if (le(sE2, -ct)) {
+        deldelh = imin(deldelh, hR);
+        deldelh = imax(deldelh, hsd / sE2);
+    }
+    const double pl = flip(hL * delb, true), pr = flip(hR * delb, true);
+    deldelphi = imin(deldelphi, g * imax(pl, pr));
+    deldelphi = imax(deldelphi, g * imin(pl, pr));
     double d0 = delh - deldelh, d1 = delhu, d2 = delphi - deldelphi;
 
-    double det = det3(r00, r01, r02, r10, r11, r12, r20, r21, r22);
-    double beta0 = det3(d0, r01, r02, d1, r11, r12, d2, r21, r22) / det;
-    double beta1 = det3(r00, d0, r02, r10, d1, r12, r20, d2, r22) / det;
-    double beta2 = det3(r00, r01, d0, r10, r11, d1, r20, r21, d2) / det;
+    double beta0, beta1, beta2;
+    const double det = l0 - l2;
+    const bool quick = moderate(l0) && moderate(l2) && moderate(d0) && moderate(d1) && moderate(d2) &&
+                       (dbits(det) << 1) != 0;
+    // beta1's numerator, the source's expression with the products by 1 dropped
+    const double n1 = ((d1 * r22 - l2 * d2) - d0 * (l0 * r22 - l2 * r20)) + (l0 * d2 - d1 * r20);
+    if (quick) {
+        const Recip rd{det, flip(rsp.y, true), rsp.fast};  // RN(1 / det) = -RN(1 / (sE2 - sE1))
+        beta0 = div_rn(d1 - d0 * l2, rd);
+        beta1 = div_rn(n1, rd);
+        beta2 = div_rn(d0 * l0 - d1, rd);
+    } else {
+        const double r00 = 1.0, r01 = 0.0, r02 = 1.0, r10 = l0, r11 = 0.0, r12 = l2, r21 = 1.0;
+        const double dt = det3(r00, r01, r02, r10, r11, r12, r20, r21, r22);
+        beta0 = det3(d0, r01, r02, d1, r11, r12, d2, r21, r22) / dt;
+        beta1 = det3(r00, d0, r02, r10, d1, r12, r20, d2, r22) / dt;
+        beta2 = det3(r00, r01, d0, r10, r11, d1, r20, r21, d2) / dt;
+    }
 
     sw[0] = l0;
     sw[1] = l1;
     sw[2] = l2;
-    fw[0][0] = beta0 * r10; fw[1][0] = beta0 * r20; fw[2][0] = beta0 * r10;
-    fw[0][1] = beta1 * r11; fw[1][1] = beta1 * r21; fw[2][1] = beta1 * r11;
-    fw[0][2] = beta2 * r12; fw[1][2] = beta2 * r22; fw[2][2] = beta2 * r12;
-    fw[2][0] = fw[2][0] * vL;
-    fw[2][2] = fw[2][2] * vR;
+    // f-waves: beta times rows 2 and 3 of R (r11 = 0, r21 = 1)
+    fw[0][0] = beta0 * l0; fw[1][0] = beta0 * r20; fw[2][0] = (beta0 * l0) * vL;
+    fw[0][1] = mul0(beta1); fw[1][1] = beta1;
+    fw[0][2] = beta2 * l2; fw[1][2] = beta2 * r22; fw[2][2] = (beta2 * l2) * vR;
     fw[2][1] = ((((hR * uR) * vR) - ((hL * uL) * vL)) - fw[2][0]) - fw[2][2];
 }
 
@@ -419,7 +495,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     bool wall_l = false, wall_r = false;  // wall(1) = 0 resp. wall(3) = 0 (wall(2) = 0 with either)
     if (!wetR0) {  // hR is now 0.0, and 0.0 <= drytol
         double hstar, s1m, s2m;
-        riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);
+        riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);  // a rare edge: sqrt here
         double hstartest = dmx(hL, hstar);
         if (hstartest + bL < bR) {
             wall_r = true;
@@ -429,7 +505,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         }
     } else if (!wetL0) {
         double hstar, s1m, s2m;
-        riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);
+        riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);  // a rare edge: sqrt here
         double hstartest = dmx(hR, hstar);
         if (hstartest + bR < bL) {
             wall_l = true;
@@ -458,7 +534,11 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
 
     double sw[3], fw[3][3];
     if (SOLVER == AUG_RIEMANN) {
-        riemann_aug(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR, drytol, sw, fw);
+        // RN(1 / h) of the fixed-up depths: a wet side's own, a wall's mirrored one
+        const double yLf = wall_l ? yR0 : yL0, yRf = wall_r ? yL0 : yR0;
+        const bool okL = wetL && recip_fast(hL), okR = wetR && recip_fast(hR);
+        riemann_aug(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR, yLf, yRf, okL, okR,
+                    drytol, sw, fw);
     } else {
         double delhu = huR - huL;
         double delb = bR - bL;

@@ -262,7 +262,7 @@ def test_riemann_batch_against_oracle(swe_lib, oracle_lib):
     import ctypes as C
     from samoa_gb300 import _lib
     rng = np.random.default_rng(11)
-    n = 4000
+    n = 20000
     normals = rng.normal(size=(n, 2))
     normals /= np.linalg.norm(normals, axis=1, keepdims=True)
     bl = rng.uniform(-20, 5, n)
@@ -271,6 +271,23 @@ def test_riemann_batch_against_oracle(swe_lib, oracle_lib):
     dr = rng.choice([0.0, 1e-4, 1.0], n, p=[0.2, 0.1, 0.7]) * rng.uniform(0, 20, n)
     ql = np.stack([bl + dl, rng.normal(0, 30, n), rng.normal(0, 30, n), bl], 1)
     qr = np.stack([br + dr, rng.normal(0, 30, n), rng.normal(0, 30, n), br], 1)
+    # degenerate families: water at rest (zero momenta), equal depths, identical
+    # states, slow flow over equal bottoms (zero and near-zero Cramer numerators,
+    # sonic tests on both sides of their thresholds)
+    m = n // 5
+    k = np.arange(n)
+    rest = k % 5 == 0
+    ql[rest, 1:3] = 0.0
+    qr[rest, 1:3] = 0.0
+    eqd = k % 5 == 1
+    qr[eqd, 0] = qr[eqd, 3] + (ql[eqd, 0] - ql[eqd, 3])
+    same = k % 5 == 2
+    qr[same] = ql[same]
+    slow = k % 5 == 3
+    qr[slow, 3] = ql[slow, 3]
+    ql[slow, 1:3] = rng.normal(0, 1e-7, (int(slow.sum()), 2))
+    qr[slow, 1:3] = rng.normal(0, 1e-7, (int(slow.sum()), 2))
+    assert m > 0
     drytol = 1e-3
     L = _lib.load()
     for solver in (swe.FWAVE, swe.AUG_RIEMANN, swe.LF_BATH, swe.LLF_BATH):
