@@ -41,6 +41,9 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--log2-cells", type=int, default=26)
     ap.add_argument("--solver", default="fwave")
+    ap.add_argument("--workload", default="basin", choices=["basin", "bowl"],
+                    help="basin: the synthetic ocean basin (the headline); bowl: the wet/dry parabolic bowl, "
+                         "half dry land (a parity case, for profiling the wet/dry paths and the solvers)")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-tune", action="store_true", help="skip the tiling autotuner (default tiling)")
     ap.add_argument("--no-adaptive", action="store_true")
@@ -401,7 +404,10 @@ def run_gpu(a, rank, world, local):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    scn = scenarios.ocean_basin(log2_cells=a.log2_cells, solver=a.solver, device="cuda")
+    if a.workload == "bowl":
+        scn = scenarios.parabolic_bowl(log2_cells=a.log2_cells, solver=a.solver, amplitude=2.0, sigma=0.08)
+    else:
+        scn = scenarios.ocean_basin(log2_cells=a.log2_cells, solver=a.solver, device="cuda")
     g = scn.grid
     n = g.mesh.n_cells
     ctx = swe.SweContext(local)
@@ -549,7 +555,8 @@ def run_gpu(a, rank, world, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "cells": n,
+            "config": {"workload": ("ocean_basin_2^%d_cells_%s_fp64" if a.workload == "basin" else
+                                    "parabolic_bowl_2^%d_cells_%s_fp64") % (a.log2_cells, a.solver), "cells": n,
                        "solver": a.solver, "boundary": "outflow", "segment_cells": tiling[0],
                        "block_threads": tiling[1], "staging_depth": tuning["best"][2] if tuning else 1,
                        "arith": a.arith, "autotune": tuning, "cross_segment_edges": counts["cross_edges"],

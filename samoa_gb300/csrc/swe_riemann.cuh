@@ -687,27 +687,34 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
 __device__ __forceinline__ double normal_velocity(double n1, double n2, double p1, double p2, double d) {
     return z0(n1 * (p1 / d)) + n2 * (p2 / d);
 }
+// The same with the quotients from r = {d, RN(1 / d)} (div_rn: IEEE results).
+__device__ __forceinline__ double normal_velocity(double n1, double n2, double p1, double p2, const Recip& r) {
+    return z0(n1 * div_rn(p1, r)) + n2 * div_rn(p2, r);
+}
 
 // compute_lf_flux, src/SWE/SWE_euler_timestep.f90:359-446
+// yL / yR: RN(1 / depth) of the two states where the depth is above the dry
+// tolerance (else not read).
 template <int SOLVER>
 __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, const State& QR, double dL,
-                                        double dR, double drytol, Update& fL, Update& fR) {
+                                        double dR, double drytol, Update& fL, Update& fR, double yL, double yR) {
     const double g = kG;
     if (SOLVER == LF_BATH || SOLVER == LLF_BATH) {
+        const Recip rL{dL, yL, lt(drytol, dL) && recip_fast(dL)}, rR{dR, yR, lt(drytol, dR) && recip_fast(dR)};
         if (dL < drytol || dR < drytol) {
             fL = Update{0.0, 0.0, 0.0, 0.0};
             fR = Update{0.0, 0.0, 0.0, 0.0};
             if (dL < drytol && dR < drytol) {
             } else if (dL < drytol) {
                 double hR = dmx(dR, 0.0);
-                double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+                double vR = normal_velocity(n1, n2, QR.p1, QR.p2, rR);
                 fR.s = sqrt(g * hR) + fabs(vR);
                 double pr = ((0.5 * g) * hR) * hR;
                 fR.p1 = (-((0.5 * vR) * QR.p1) - pr * n1) + (0.5 * fR.s) * QR.p1;
                 fR.p2 = (-((0.5 * vR) * QR.p2) - pr * n2) + (0.5 * fR.s) * QR.p2;
             } else {
                 double hL = dmx(dL, 0.0);
-                double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
+                double vL = normal_velocity(n1, n2, QL.p1, QL.p2, rL);
                 fL.s = sqrt(g * hL) + fabs(vL);
                 double pr = ((0.5 * g) * hL) * hL;
                 fL.p1 = ((0.5 * vL) * QL.p1 + pr * n1) + (0.5 * fL.s) * QL.p1;
@@ -716,8 +723,8 @@ __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, c
             return;
         }
         double hL = dmx(dL, 0.0), hR = dmx(dR, 0.0);
-        double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
-        double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+        double vL = normal_velocity(n1, n2, QL.p1, QL.p2, rL);
+        double vR = normal_velocity(n1, n2, QR.p1, QR.p2, rR);
         fL.s = sqrt(g * hL) + fabs(vL);
         fR.s = sqrt(g * hR) + fabs(vR);
         double alpha = (SOLVER == LLF_BATH) ? dmx(fL.s, fR.s) : 100.0;
@@ -763,7 +770,7 @@ __device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL,
     if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
         geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, axis);
     else
-        lf_flux<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, fL, fR);
+        lf_flux<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, fL, fR, yL, yR);
 }
 
 // depth, sqrt(g * depth) and RN(1 / depth) of a state, as the edge code needs them
