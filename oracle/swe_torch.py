@@ -9,10 +9,11 @@ gradient through torch.autograd, with the dt sequence frozen and every branch
 (wet/dry, wave-speed signs, min/max) differentiated on the side taken, is the
 FP64 CPU reference for the GPU's hand-written discrete adjoint.
 
-Only the f-wave solver with OUTFLOW, SLIP or NOSLIP walls is restated here;
-wall reconstruction at wet/dry edges (the riemanntype branch) is covered: its
-condition is evaluated like the solver does and its value changes are
-differentiated.
+The f-wave solver and the four Lax-Friedrichs fluxes (compute_lf_flux,
+src/SWE/SWE_euler_timestep.f90:359-446) are restated, with OUTFLOW, SLIP or
+NOSLIP walls; wall reconstruction at wet/dry edges (the riemanntype branch) is
+covered: its condition is evaluated like the solver does and its value changes
+are differentiated.
 """
 import math
 
@@ -212,15 +213,80 @@ def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
     return fL, fR
 
 
+FWAVE, AUG_RIEMANN, LF, LF_BATH, LLF, LLF_BATH = 1, 3, 10, 11, 12, 13
+SOLVERS = {"fwave": FWAVE, "hlle": FWAVE, "aug_riemann": AUG_RIEMANN, "lf": LF, "lfbath": LF_BATH, "llf": LLF,
+           "llfbath": LLF_BATH}
+
+
+def lf_flux(solver, n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
+    """compute_lf_flux (src/SWE/SWE_euler_timestep.f90:359-446), vectorised over
+    edges, the same expressions as the oracle's: LF / LLF with or without the
+    well-balanced bathymetry terms, the dry-side fluxes of the bathymetry
+    variants. Returns the left and right fluxes (h, hu, hv)."""
+    g = G
+    zero = torch.zeros_like(hsL)
+    one = torch.ones_like(hsL)
+
+    def nv(px, py, d):  # z0(n1 * (p1 / d)) + n2 * (p2 / d): the +0 start changes no value
+        return n1 * (px / d) + n2 * (py / d)
+
+    local = solver in (LLF, LLF_BATH)
+    if solver in (LF_BATH, LLF_BATH):
+        dL, dR = hsL - bL, hsR - bR
+        dryL = _cmp(tape, dL < drytol)
+        dryR = _cmp(tape, dR < drytol)
+        dLs, dRs = _where(dryL, one, dL), _where(dryR, one, dR)  # a dry side's values are not used
+        hL, hR = _dmx(dL, zero), _dmx(dR, zero)
+        vL, vR = nv(pxL, pyL, dLs), nv(pxR, pyR, dRs)
+        sL = _sqrt(g * hL) + torch.abs(vL)
+        sR = _sqrt(g * hR) + torch.abs(vR)
+        alpha = _where(_cmp(tape, sL > sR), sL, sR) if local else 100.0 * one
+        Fh = 0.5 * ((hL * vL + hR * vR) + alpha * (hsL - hsR))
+        pr = (0.5 * g) * (hL * hL + hR * hR)
+        Fp1 = 0.5 * (((pxL * vL + pxR * vR) + pr * n1) + alpha * (pxL - pxR))
+        Fp2 = 0.5 * (((pyL * vL + pyR * vR) + pr * n2) + alpha * (pyL - pyR))
+        src = ((0.25 * g) * (hL + hR)) * (bR - bL)
+        wetL = (Fh, Fp1 + src * n1, Fp2 + src * n2)
+        wetR = (-Fh, -Fp1 + src * n1, -Fp2 + src * n2)
+        prR, prL = ((0.5 * g) * hR) * hR, ((0.5 * g) * hL) * hL
+        onlyR = (zero, (-((0.5 * vR) * pxR) - prR * n1) + (0.5 * sR) * pxR,
+                 (-((0.5 * vR) * pyR) - prR * n2) + (0.5 * sR) * pyR)
+        onlyL = (zero, ((0.5 * vL) * pxL + prL * n1) + (0.5 * sL) * pxL,
+                 ((0.5 * vL) * pyL + prL * n2) + (0.5 * sL) * pyL)
+        both = dryL & dryR
+        fL = tuple(_where(dryL | dryR, _where(dryL, zero, a), w) for a, w in zip(onlyL, wetL))
+        fR = tuple(_where(dryL | dryR, _where(both | dryR, zero, a), w) for a, w in zip(onlyR, wetR))
+        return fL, fR
+    dL, dR = hsL - 0.0, hsR - 0.0
+    hL, hR = _dmx(dL, zero), _dmx(dR, zero)
+    vL, vR = nv(pxL, pyL, dL), nv(pxR, pyR, dR)
+    sL = _sqrt(g * dL) + torch.abs(vL)
+    sR = _sqrt(g * dR) + torch.abs(vR)
+    alpha = _where(_cmp(tape, sL > sR), sL, sR) if local else 100.0 * one
+    Fh = 0.5 * ((vL * hL + vR * hR) + alpha * (hsL - hsR))
+    sc = (vL * vL) * hL + (vR * vR) * hR
+    pr = (0.5 * g) * (hL * hL + hR * hR)
+    Fp1 = 0.5 * ((sc + pr * n1) + alpha * (pxL - pxR))
+    Fp2 = 0.5 * ((sc + pr * n2) + alpha * (pyL - pyR))
+    return (Fh, Fp1, Fp2), (-Fh, -Fp1, -Fp2)
+
+
 class TorchStep:
-    """The step on a fixed mesh (C-ABI layout), f-wave, differentiable.
+    """The step on a fixed mesh (C-ABI layout), f-wave or a Lax-Friedrichs flux, differentiable.
 
     Edges are oriented by the step parity exactly like the GPU kernel; ``step``
     applies one Euler step with a given dt to (h, hu, hv) for bathymetry b.
     """
 
-    def __init__(self, mesh, scaling=1.0, drytol=0.01, bc="outflow"):
+    def __init__(self, mesh, scaling=1.0, drytol=0.01, bc="outflow", solver="fwave"):
         from oracle import oracle as O
+        sid = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        if sid == FWAVE:
+            self.flux = fwave_flux
+        elif sid in (LF, LF_BATH, LLF, LLF_BATH):
+            self.flux = lambda *a, **k: lf_flux(sid, *a, **k)
+        else:
+            raise ValueError("solver %r is not restated here" % (solver,))
         self.n = mesh.n_cells
         self.drytol = drytol
         self.bc = bc
@@ -254,8 +320,8 @@ class TorchStep:
             L, R, iL, iR, nn = self.eb, self.ea, self.lb, self.la, self.nB
         else:
             L, R, iL, iR, nn = self.ea, self.eb, self.la, self.lb, self.nA
-        fL, fR = fwave_flux(nn[:, 0], nn[:, 1], h[L], hu[L], hv[L], b[L], h[R], hu[R], hv[R], b[R], self.drytol,
-                            tape)
+        fL, fR = self.flux(nn[:, 0], nn[:, 1], h[L], hu[L], hv[L], b[L], h[R], hu[R], hv[R], b[R], self.drytol,
+                           tape)
         c = self.bcell
         n1, n2 = self.nBnd[:, 0], self.nBnd[:, 1]
         gp1, gp2 = hu[c], hv[c]
@@ -264,7 +330,7 @@ class TorchStep:
             gp1, gp2 = hu[c] - dd * n1, hv[c] - dd * n2
         elif self.bc == "noslip":
             gp1, gp2 = -hu[c], -hv[c]
-        fB, _ = fwave_flux(n1, n2, h[c], hu[c], hv[c], b[c], h[c], gp1, gp2, b[c], self.drytol, tape)
+        fB, _ = self.flux(n1, n2, h[c], hu[c], hv[c], b[c], h[c], gp1, gp2, b[c], self.drytol, tape)
         # slot values [cell, local edge]
         slots = []
         for q in range(3):

@@ -270,6 +270,145 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     }
 }
 
+// VJP of the Lax-Friedrichs fluxes (compute_lf_flux, src/SWE/SWE_euler_timestep.f90:359-446):
+// with the cotangents gL / gR of the left/right (h, hu, hv) updates, add the
+// cotangents of the two states (h = surface, hu, hv, b) to outL / outR. Every
+// max, |v| and the dry-side tests are differentiated on the branch taken; the
+// maximum wave speed matters where it enters the flux (the dry-side momentum
+// flux and the local LF alpha).
+__device__ __forceinline__ double sgn(double x) { return lt0(x) ? -1.0 : (gt0(x) ? 1.0 : 0.0); }
+
+// Normal velocity v = n1 (p1 / d) + n2 (p2 / d): adds its cotangent bv to p1, p2 and d.
+__device__ __forceinline__ void nv_vjp(double n1, double n2, double v, double d, double bv, double& bp1,
+                                       double& bp2, double& bd) {
+    const double r = 1.0 / d;
+    bp1 = fma(bv * n1, r, bp1);
+    bp2 = fma(bv * n2, r, bp2);
+    bd = fma(-bv * v, r, bd);
+}
+
+// d sqrt(g h) / dh times bs (0 where h = 0, as the reference gradient has it)
+__device__ __forceinline__ double sqrt_g_vjp(double h, double bs) {
+    return gt0(h) ? bs * (0.5 * kG) / sqrt(kG * h) : 0.0;
+}
+
+template <int SOLVER>
+__device__ __forceinline__ void lf_vjp(double n1, double n2, const State& QL, const State& QR, double dL0,
+                                       double dR0, double drytol, const double gL[3], const double gR[3],
+                                       Grad4& outL, Grad4& outR) {
+    const double g = kG;
+    if (SOLVER == LF_BATH || SOLVER == LLF_BATH) {
+        const double dL = dL0, dR = dR0;
+        const bool dryL = dL < drytol, dryR = dR < drytol;
+        if (dryL || dryR) {
+            if (dryL && dryR) return;
+            // one wet side W: f_W.p = s_W (+-0.5 v_W p - pr n) + 0.5 sp p, f_W.h = 0
+            const bool right = dryL;
+            const State& Q = right ? QR : QL;
+            const double d = right ? dR : dL;
+            const double* gg = right ? gR : gL;
+            const double sgw = right ? -1.0 : 1.0;  // fR: -(0.5 v p) - pr n; fL: +(0.5 v p) + pr n
+            const double hw = dmx(d, 0.0);
+            const double v = normal_velocity(n1, n2, Q.p1, Q.p2, d);
+            const double sp = sqrt(g * hw) + fabs(v);
+            double b_v = sgw * 0.5 * fma(gg[1], Q.p1, gg[2] * Q.p2);
+            const double b_pr = sgw * fma(gg[1], n1, gg[2] * n2);
+            const double b_sp = 0.5 * fma(gg[1], Q.p1, gg[2] * Q.p2);
+            const double k = fma(sgw * 0.5, v, 0.5 * sp);
+            double b_p1 = gg[1] * k, b_p2 = gg[2] * k;
+            double b_h = b_pr * (g * hw) + sqrt_g_vjp(hw, b_sp);
+            b_v = fma(b_sp, sgn(v), b_v);
+            double b_d = gt0(d) ? b_h : 0.0;
+            nv_vjp(n1, n2, v, d, b_v, b_p1, b_p2, b_d);
+            Grad4& o = right ? outR : outL;
+            o.h += b_d;
+            o.hu += b_p1;
+            o.hv += b_p2;
+            o.b -= b_d;
+            return;
+        }
+        const double hL = dmx(dL, 0.0), hR = dmx(dR, 0.0);
+        const double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
+        const double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+        const double sL = sqrt(g * hL) + fabs(vL), sR = sqrt(g * hR) + fabs(vR);
+        const bool left_max = sL > sR;
+        const double alpha = (SOLVER == LLF_BATH) ? (left_max ? sL : sR) : 100.0;
+        // fL = (F_h, F_p1 + src n1, F_p2 + src n2), fR = (-F_h, -F_p1 + src n1, -F_p2 + src n2)
+        const double bFh = gL[0] - gR[0], bF1 = gL[1] - gR[1], bF2 = gL[2] - gR[2];
+        const double b_src = fma(gL[1] + gR[1], n1, (gL[2] + gR[2]) * n2);
+        double b_hL = 0.5 * bFh * vL, b_hR = 0.5 * bFh * vR;
+        double b_vL = 0.5 * fma(bFh, hL, fma(bF1, QL.p1, bF2 * QL.p2));
+        double b_vR = 0.5 * fma(bFh, hR, fma(bF1, QR.p1, bF2 * QR.p2));
+        const double b_alpha = 0.5 * fma(bFh, QL.h - QR.h, fma(bF1, QL.p1 - QR.p1, bF2 * (QL.p2 - QR.p2)));
+        double b_hsL = 0.5 * bFh * alpha, b_hsR = -0.5 * bFh * alpha;
+        double b_pL1 = 0.5 * bF1 * (vL + alpha), b_pR1 = 0.5 * bF1 * (vR - alpha);
+        double b_pL2 = 0.5 * bF2 * (vL + alpha), b_pR2 = 0.5 * bF2 * (vR - alpha);
+        const double b_pr = 0.5 * fma(bF1, n1, bF2 * n2);
+        b_hL = fma(b_pr * g, hL, b_hL);
+        b_hR = fma(b_pr * g, hR, b_hR);
+        const double cs = (0.25 * g) * (QR.b - QL.b), ch = (0.25 * g) * (hL + hR);
+        b_hL = fma(b_src, cs, b_hL);
+        b_hR = fma(b_src, cs, b_hR);
+        double b_bR = b_src * ch, b_bL = -b_src * ch;
+        double b_sL = 0.0, b_sR = 0.0;
+        if (SOLVER == LLF_BATH) {
+            if (left_max) b_sL = b_alpha;
+            else b_sR = b_alpha;
+        }
+        b_hL += sqrt_g_vjp(hL, b_sL);
+        b_hR += sqrt_g_vjp(hR, b_sR);
+        b_vL = fma(b_sL, sgn(vL), b_vL);
+        b_vR = fma(b_sR, sgn(vR), b_vR);
+        double b_dL = gt0(dL) ? b_hL : 0.0, b_dR = gt0(dR) ? b_hR : 0.0;
+        nv_vjp(n1, n2, vL, dL, b_vL, b_pL1, b_pL2, b_dL);
+        nv_vjp(n1, n2, vR, dR, b_vR, b_pR1, b_pR2, b_dR);
+        outL.h += b_hsL + b_dL;
+        outL.hu += b_pL1;
+        outL.hv += b_pL2;
+        outL.b += b_bL - b_dL;
+        outR.h += b_hsR + b_dR;
+        outR.hu += b_pR1;
+        outR.hv += b_pR2;
+        outR.b += b_bR - b_dR;
+    } else {
+        // no bathymetry: depth = surface
+        const double dL = QL.h - 0.0, dR = QR.h - 0.0;
+        const double hL = dmx(dL, 0.0), hR = dmx(dR, 0.0);
+        const double vL = normal_velocity(n1, n2, QL.p1, QL.p2, dL);
+        const double vR = normal_velocity(n1, n2, QR.p1, QR.p2, dR);
+        const double sL = sqrt(g * dL) + fabs(vL), sR = sqrt(g * dR) + fabs(vR);
+        const bool left_max = sL > sR;
+        const double alpha = (SOLVER == LLF) ? (left_max ? sL : sR) : 100.0;
+        const double bFh = gL[0] - gR[0], bF1 = gL[1] - gR[1], bF2 = gL[2] - gR[2];
+        const double b_sc = 0.5 * (bF1 + bF2);
+        const double b_pr = 0.5 * fma(bF1, n1, bF2 * n2);
+        const double b_alpha = 0.5 * fma(bFh, QL.h - QR.h, fma(bF1, QL.p1 - QR.p1, bF2 * (QL.p2 - QR.p2)));
+        double b_hsL = 0.5 * bFh * alpha, b_hsR = -0.5 * bFh * alpha;
+        double b_pL1 = 0.5 * bF1 * alpha, b_pR1 = -0.5 * bF1 * alpha;
+        double b_pL2 = 0.5 * bF2 * alpha, b_pR2 = -0.5 * bF2 * alpha;
+        double b_vL = fma(0.5 * bFh, hL, b_sc * 2.0 * vL * hL), b_vR = fma(0.5 * bFh, hR, b_sc * 2.0 * vR * hR);
+        double b_hL = fma(0.5 * bFh, vL, fma(b_sc, vL * vL, b_pr * g * hL));
+        double b_hR = fma(0.5 * bFh, vR, fma(b_sc, vR * vR, b_pr * g * hR));
+        double b_sL = 0.0, b_sR = 0.0;
+        if (SOLVER == LLF) {
+            if (left_max) b_sL = b_alpha;
+            else b_sR = b_alpha;
+        }
+        b_vL = fma(b_sL, sgn(vL), b_vL);
+        b_vR = fma(b_sR, sgn(vR), b_vR);
+        double b_dL = (gt0(dL) ? b_hL : 0.0) + sqrt_g_vjp(dL, b_sL);
+        double b_dR = (gt0(dR) ? b_hR : 0.0) + sqrt_g_vjp(dR, b_sR);
+        nv_vjp(n1, n2, vL, dL, b_vL, b_pL1, b_pL2, b_dL);
+        nv_vjp(n1, n2, vR, dR, b_vR, b_pR1, b_pR2, b_dR);
+        outL.h += b_hsL + b_dL;
+        outL.hu += b_pL1;
+        outL.hv += b_pL2;
+        outR.h += b_hsR + b_dR;
+        outR.hu += b_pR1;
+        outR.hv += b_pR2;
+    }
+}
+
 // Cotangent of a boundary ghost state pulled back to the cell (the ghost of
 // bnd_skeleton_scalar_op is a linear function of the cell state).
 template <int BC>
@@ -324,6 +463,16 @@ __device__ __forceinline__ void cell_mu(const AdjointArgs& A, int c, double ndv,
     }
 }
 
+// The edge VJP of the step's flux for each solver.
+template <int SOLVER>
+__device__ __forceinline__ void edge_vjp(double n1, double n2, const State& QL, const State& QR, double dL,
+                                         double dR, double sqL, double sqR, double yL, double yR, double drytol,
+                                         const double gL[3], const double gR[3], Grad4& oL, Grad4& oR, int axis) {
+    if (SOLVER == FWAVE) fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, gL, gR, oL, oR, axis);
+    else lf_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, gL, gR, oL, oR);
+}
+
+template <int SOLVER>
 __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int T = A.seg_cells;
@@ -435,7 +584,8 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                 gR[2] = lenR * mR[2];
             }
             Grad4 oL{0.0, 0.0, 0.0, 0.0}, oR{0.0, 0.0, 0.0, 0.0};
-            fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR, (int)((meta >> 15) & 3u));
+            edge_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR,
+                             (int)((meta >> 15) & 3u));
             if (bnd) {  // the ghost's cotangent goes back to the cell
                 if (P.bc == BC_SLIP) boundary_ghost_vjp<BC_SLIP>(n1, n2, oR, oL);
                 else if (P.bc == BC_NOSLIP) boundary_ghost_vjp<BC_NOSLIP>(n1, n2, oR, oL);

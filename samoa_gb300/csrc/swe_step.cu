@@ -282,6 +282,7 @@ struct swe_ctx {
     std::vector<InstParams> ip_host;
     int adj_grid = 0;               // adjoint launch shape for the current tiling (0 = not configured)
     int32_t adj_seg_cells = 0;
+    int adj_solver = 0;
     // CUDA graphs of n steps
     std::map<int64_t, cudaGraphExec_t> graphs;
     double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
@@ -1145,6 +1146,19 @@ int swe_step_back(swe_ctx* c) {
 }  // extern "C"
 
 namespace {
+typedef void (*AdjKernel)(AdjointArgs);
+// The reverse step for the solvers the adjoint differentiates (else null).
+AdjKernel adjoint_kernel_for(int solver) {
+    switch (solver) {
+        case FWAVE: return adjoint_kernel<FWAVE>;
+        case LF: return adjoint_kernel<LF>;
+        case LF_BATH: return adjoint_kernel<LF_BATH>;
+        case LLF: return adjoint_kernel<LLF>;
+        case LLF_BATH: return adjoint_kernel<LLF_BATH>;
+        default: return nullptr;
+    }
+}
+
 // The reverse of step t (the context's state is x_t, parity t & 1).
 int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double* lam_h, const double* lam_hu,
                    const double* lam_hv, double* out_h, double* out_hu, double* out_hv, double* bbar) {
@@ -1178,15 +1192,19 @@ int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double*
     // 256 threads per CTA so an SM still has two CTAs' worth of warps
     const int threads = 256;
     const size_t smem = (size_t)21 * c->seg_cells * sizeof(double);
-    if (c->adj_seg_cells != c->seg_cells) {
-        CUDA_TRY(cudaFuncSetAttribute(adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int solver = c->params[0].solver;
+    const AdjKernel kern = adjoint_kernel_for(solver);
+    if (!kern) return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave and Lax-Friedrichs fluxes");
+    if (c->adj_seg_cells != c->seg_cells || c->adj_solver != solver) {
+        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, threads, smem));
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
         if (per_sm < 1) return set_error(SWE_E_INVALID, "adjoint tiling does not fit an SM");
         c->adj_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * c->num_sms, c->n_seg));
         c->adj_seg_cells = c->seg_cells;
+        c->adj_solver = solver;
     }
-    adjoint_kernel<<<c->adj_grid, threads, smem, c->stream>>>(A);
+    kern<<<c->adj_grid, threads, smem, c->stream>>>(A);
     CUDA_TRY(cudaGetLastError());
     return SWE_OK;
 }
@@ -1199,8 +1217,8 @@ int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, con
     int rc = ready(c);
     if (rc) return rc;
     if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
-    if (c->params[0].solver != SWE_SOLVER_FWAVE)
-        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave solver");
+    if (!adjoint_kernel_for(c->params[0].solver))
+        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave and Lax-Friedrichs fluxes");
     if (!lam_h || !lam_hu || !lam_hv || !out_h || !out_hu || !out_hv || !bbar)
         return set_error(SWE_E_INVALID, "null cotangent buffer");
     cudaSetDevice(c->device);
@@ -1509,8 +1527,8 @@ int swe_gauge_gradient(swe_ctx* c, int64_t n_steps, const double* dts, int32_t s
     int rc = ready(c);
     if (rc) return rc;
     if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
-    if (c->params[0].solver != SWE_SOLVER_FWAVE)
-        return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave solver");
+    if (!adjoint_kernel_for(c->params[0].solver))
+        return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave and Lax-Friedrichs fluxes");
     if (n_steps < 1 || !dts || snapshots < 1 || n_gauges < 1 || !gauges || !obs || !grad_h || !grad_b || !J)
         return set_error(SWE_E_INVALID, "bad arguments");
     cudaSetDevice(c->device);
