@@ -9,8 +9,9 @@ gradient through torch.autograd, with the dt sequence frozen and every branch
 (wet/dry, wave-speed signs, min/max) differentiated on the side taken, is the
 FP64 CPU reference for the GPU's hand-written discrete adjoint.
 
-The f-wave solver and the four Lax-Friedrichs fluxes (compute_lf_flux,
-src/SWE/SWE_euler_timestep.f90:359-446) are restated, with OUTFLOW, SLIP or
+The f-wave solver, the augmented solver (riemann_aug_JCP with riemanntype,
+src/geoclaw/riemannsolvers.f:2-258,507-618) and the four Lax-Friedrichs fluxes
+(compute_lf_flux, src/SWE/SWE_euler_timestep.f90:359-446) are restated, with OUTFLOW, SLIP or
 NOSLIP walls; wall reconstruction at wet/dry edges (the riemanntype branch) is
 covered: its condition is evaluated like the solver does and its value changes
 are differentiated.
@@ -121,9 +122,165 @@ def _riemann_structure_hstar(hL, hR, uL, uR, drytol):
     return torch.where(h_min <= drytol, torch.zeros_like(hm), hm)
 
 
+def _fwave_core(v, tape):
+    """riemann_fwave (src/geoclaw/riemannsolvers.f:446-500): speeds and f-waves
+    from the wrapper's values v (a dict)."""
+    g = G
+    zero, one = v["zero"], v["one"]
+    hL, hR, huL, huR, bL, bR = v["hL"], v["hR"], v["huL"], v["huR"], v["bL"], v["bR"]
+    vL, vR, sE1, sE2, delphi = v["vL"], v["vR"], v["sE1"], v["sE2"], v["delphi"]
+    delhu = huR - huL
+    delb = bR - bL
+    deldelphi = -(((g * 0.5) * (hR + hL)) * delb)
+    dpd = delphi - deldelphi
+    ds = sE2 - sE1
+    ds = _where(ds != 0, ds, one)
+    beta1 = (sE2 * delhu - dpd) / ds
+    beta2 = (dpd - sE1 * delhu) / ds
+    sw = [sE1, 0.5 * (sE1 + sE2), sE2]
+    fw = [[beta1, zero, beta2], [beta1 * sE1, zero, beta2 * sE2], [beta1 * vL, None, beta2 * vR]]
+    fw[2][1] = ((huR * vR - huL * vL) - fw[2][0]) - fw[2][2]
+    return sw, fw
+
+
+def _tmin(tape, a, b):  # dmn(a, b) = (a < b) ? a : b, the comparison on the tape
+    return torch.where(_cmp(tape, a < b), a, b)
+
+
+def _tmax(tape, a, b):  # dmx(a, b) = (a > b) ? a : b
+    return torch.where(_cmp(tape, a > b), a, b)
+
+
+def _riemann_structure(hL, hR, uL, uR, sqL, sqR, drytol, tape, one):
+    """riemanntype (src/geoclaw/riemannsolvers.f:507-618) with one Newton step,
+    differentiable: every branch is evaluated on safe operands where it is not
+    taken and the taken one selected. sqL / sqR are sqrt(g h) of hL / hR.
+    Returns (s1m, s2m)."""
+    g = G
+    lowR = _cmp(tape, hR < hL)    # h_min = dmn(hR, hL) is hR
+    highR = _cmp(tape, hR > hL)   # h_max = dmx(hR, hL) is hR
+    h_min, h_max = _where(lowR, hR, hL), _where(highR, hR, hL)
+    sq_min, sq_max = _where(lowR, sqR, sqL), _where(highR, sqR, sqL)
+    delu = uR - uL
+    dry = _cmp(tape, h_min <= drytol)
+    t_dry = ((uR + uL) - 2.0 * sqR) + 2.0 * sqL
+    hmn, hmx = _where(dry, one, h_min), _where(dry, one, h_max)
+    hLs, hRs = _where(dry, one, hL), _where(dry, one, hR)
+    F_min = delu + 2.0 * (sq_min - sq_max)
+    F_max = delu + (hmx - hmn) * _sqrt(((0.5 * g) * (hmx + hmn)) / (hmx * hmn))
+    rare = _cmp(tape, F_min > 0.0)
+    shock = _cmp(tape, F_max <= 0.0)
+    # two rarefactions
+    t = _tmax(tape, torch.zeros_like(delu), -delu + 2.0 * (sqL + sqR))
+    hm_r = (1.0 / (16.0 * g)) * (t * t)
+    sqm_r = _sqrt(g * hm_r)
+    s1_r = (uL + 2.0 * sqL) - 3.0 * sqm_r
+    s2_r = (uR - 2.0 * sqR) + 3.0 * sqm_r
+    # two shocks: one Newton step on sqrt(h)
+    h0 = hmx
+    gL = _sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hLs))
+    gR = _sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hRs))
+    F0 = (delu + (h0 - hLs) * gL) + (h0 - hRs) * gR
+    dfdh = ((gL - (g * (h0 - hLs)) / ((4.0 * (h0 * h0)) * gL)) + gR) - (g * (h0 - hRs)) / ((4.0 * (h0 * h0)) * gR)
+    slope = (2.0 * _sqrt(h0)) * dfdh
+    tt = _sqrt(h0) - F0 / _where(slope != 0, slope, one)
+    hm_s = tt * tt
+    hms = _where(hm_s > 0, hm_s, one)
+    u1m = uL - (hm_s - hLs) * _sqrt((0.5 * g) * (1.0 / hms + 1.0 / hLs))
+    u2m = uR + (hm_s - hRs) * _sqrt((0.5 * g) * (1.0 / hms + 1.0 / hRs))
+    sqm_s = _sqrt(g * hm_s)
+    s1_s, s2_s = u1m - sqm_s, u2m + sqm_s
+    # one shock, one rarefaction
+    h0 = hmn
+    F0m = (delu + 2.0 * (sq_min - sq_max)) + (h0 - hmn) * _sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hmn))
+    den = hmx - hmn
+    slope_m = (F_max - F0m) / _where(den != 0, den, one)
+    hm_m = h0 - F0m / _where(slope_m != 0, slope_m, one)
+    sqm_m = _sqrt(g * _where(hm_m >= 0, hm_m, one))
+    lhigh = _cmp(tape, hL > hR)
+    s1_m = _where(lhigh, (uL + 2.0 * sqL) - 3.0 * sqm_m, (uR - 2.0 * sqR) + sqm_m)
+    s2_m = _where(lhigh, (uL + 2.0 * sqL) - sqm_m, (uR - 2.0 * sqR) + 3.0 * sqm_m)
+    s1m = _where(dry, t_dry, _where(rare, s1_r, _where(shock, s1_s, s1_m)))
+    s2m = _where(dry, t_dry, _where(rare, s2_r, _where(shock, s2_s, s2_m)))
+    return s1m, s2m
+
+
+def _det3(a00, a01, a02, a10, a11, a12, a20, a21, a22):
+    d1 = a00 * (a11 * a22 - a12 * a21)
+    d2 = a01 * (a10 * a22 - a12 * a20)
+    d3 = a02 * (a10 * a21 - a11 * a20)
+    return (d1 - d2) + d3
+
+
+def _aug_core(v, tape):
+    """riemann_aug_JCP (src/geoclaw/riemannsolvers.f:2-258) with maxiter = 1 and
+    the entropy corrector off, the oracle's expressions."""
+    g = G
+    zero, one = v["zero"], v["one"]
+    hL, hR, huL, huR, bL, bR = v["hL"], v["hR"], v["huL"], v["huR"], v["bL"], v["bR"]
+    uL, uR, vL, vR, delphi, sqL, sqR = v["uL"], v["uR"], v["vL"], v["vR"], v["delphi"], v["sqL"], v["sqR"]
+    delh, delhu, delb = hR - hL, huR - huL, bR - bL
+    s1m, s2m = _riemann_structure(hL, hR, uL, uR, sqL, sqR, v["drytol"], tape, one)
+    l0 = _tmin(tape, v["sE1"], s2m)
+    l2 = _tmax(tape, v["sE2"], s1m)
+    sE1, sE2 = l0, l2
+    dsp = sE2 - sE1
+    hstar = _tmax(tape, (((huL - huR) + sE2 * hR) - sE1 * hL) / _where(dsp != 0, dsp, one), zero)
+    l1 = 0.5 * (l0 + l2)
+    l1 = _where(_cmp(tape, torch.abs(l1) < 1e-20), zero, l1)
+    r10, r12, r20, r22 = l0, l2, l0 * l0, l2 * l2
+    ct = 1e-6
+    hbar = _tmax(tape, 0.5 * (hL + hR), zero)
+    su = uL + uR
+    s1s2bar = 0.25 * (su * su) - g * hbar
+    s1s2tilde = _tmax(tape, zero, uL * uR) - g * hbar
+    sonic = ((torch.abs(s1s2bar) <= ct) | (s1s2bar * s1s2tilde <= ct) | ((s1s2bar * sE1) * sE2 <= ct) |
+             (torch.minimum(torch.abs(sE1), torch.abs(sE2)) < ct) | ((sE1 < 0.0) & (s1m > 0.0)) |
+             ((sE2 > 0.0) & (s2m < 0.0)) | ((uL + sqL) * (uR + sqR) < 0.0) | ((uL - sqL) * (uR - sqR) < 0.0))
+    sonic = _cmp(tape, sonic)
+    sbs = _where(sonic | (s1s2bar == 0), one, s1s2bar)
+    deldelh = _where(sonic, -delb, ((delb * g) * hbar) / sbs)
+    caseA = _cmp(tape, (sE1 < -ct) & (sE2 > ct))
+    caseB = _cmp(tape, (~caseA) & (sE1 >= ct))
+    caseC = _cmp(tape, (~caseA) & (~caseB) & (sE2 <= -ct))
+    hsd = hstar * (sE2 - sE1)
+    l0s, l2s = _where(l0 != 0, l0, one), _where(l2 != 0, l2, one)
+    dA = _tmax(tape, _tmin(tape, deldelh, hsd / l2s), hsd / l0s)
+    dB = _tmax(tape, _tmin(tape, deldelh, hsd / l0s), -hL)
+    dC = _tmax(tape, _tmin(tape, deldelh, hR), hsd / l2s)
+    deldelh = _where(caseA, dA, _where(caseB, dB, _where(caseC, dC, deldelh)))
+    deldelphi = _where(sonic, -((g * hbar) * delb), -((((delb * g) * hbar) * s1s2tilde) / sbs))
+    pl, pr = -(hL * delb), -(hR * delb)
+    deldelphi = _tmin(tape, deldelphi, g * _tmax(tape, pl, pr))
+    deldelphi = _tmax(tape, deldelphi, g * _tmin(tape, pl, pr))
+    d0, d1, d2 = delh - deldelh, delhu, delphi - deldelphi
+    r00, r01, r02, r11, r21 = one, zero, one, zero, one
+    det = _det3(r00, r01, r02, r10, r11, r12, r20, r21, r22)
+    dets = _where(det != 0, det, one)
+    beta0 = _det3(d0, r01, r02, d1, r11, r12, d2, r21, r22) / dets
+    beta1 = _det3(r00, d0, r02, r10, d1, r12, r20, d2, r22) / dets
+    beta2 = _det3(r00, r01, d0, r10, r11, d1, r20, r21, d2) / dets
+    fw = [[beta0 * r10, beta1 * r11, beta2 * r12], [beta0 * r20, beta1 * r21, beta2 * r22],
+          [(beta0 * r10) * vL, None, (beta2 * r12) * vR]]
+    fw[2][1] = ((((hR * uR) * vR) - ((hL * uL) * vL)) - fw[2][0]) - fw[2][2]
+    return [l0, l1, l2], fw
+
+
+def aug_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
+    """compute_geoclaw_flux with the augmented solver, vectorised over edges."""
+    return geoclaw_flux(_aug_core, n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape)
+
+
 def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
     """compute_geoclaw_flux with the f-wave solver, vectorised over edges.
     Returns the left and right net updates (h, hu, hv) in world coordinates."""
+    return geoclaw_flux(_fwave_core, n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape)
+
+
+def geoclaw_flux(core, n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
+    """compute_geoclaw_flux (src/SWE/SWE_euler_timestep.f90:449-481) around
+    c_bind_geoclaw_solver_dp's wet/dry handling (c_bind_riemannsolvers.f90:16-176)
+    with the solver `core`, vectorised over edges."""
     g = G
     zero = torch.zeros_like(hsL)
     one = torch.ones_like(hsL)
@@ -181,17 +338,8 @@ def fwave_flux(n1, n2, hsL, pxL, pyL, bL, hsR, pxR, pyR, bR, drytol, tape=None):
     r1, r2 = uhat - chat, uhat + chat
     sE1 = _where(_cmp(tape, sL < r1), sL, r1)
     sE2 = _where(_cmp(tape, sR > r2), sR, r2)
-    delhu = huR - huL
-    delb = bR - bL
-    deldelphi = -(((g * 0.5) * (hR + hL)) * delb)
-    dpd = delphi - deldelphi
-    ds = sE2 - sE1
-    ds = _where(ds != 0, ds, one)
-    beta1 = (sE2 * delhu - dpd) / ds
-    beta2 = (dpd - sE1 * delhu) / ds
-    sw = [sE1, 0.5 * (sE1 + sE2), sE2]
-    fw = [[beta1, zero, beta2], [beta1 * sE1, zero, beta2 * sE2], [beta1 * vL, None, beta2 * vR]]
-    fw[2][1] = ((huR * vR - huL * vL) - fw[2][0]) - fw[2][2]
+    sw, fw = core(dict(zero=zero, one=one, hL=hL, hR=hR, huL=huL, huR=huR, bL=bL, bR=bR, uL=uL, uR=uR, vL=vL,
+                       vR=vR, sE1=sE1, sE2=sE2, delphi=delphi, sqL=sqL, sqR=sqR, drytol=drytol), tape)
     walls = [wall_l, wall_l | wall_r, wall_r]
     for w in range(3):
         sw[w] = _where(walls[w], sw[w] * 0.0, sw[w])
@@ -283,6 +431,8 @@ class TorchStep:
         sid = SOLVERS[solver] if isinstance(solver, str) else int(solver)
         if sid == FWAVE:
             self.flux = fwave_flux
+        elif sid == AUG_RIEMANN:
+            self.flux = aug_flux
         elif sid in (LF, LF_BATH, LLF, LLF_BATH):
             self.flux = lambda *a, **k: lf_flux(sid, *a, **k)
         else:
