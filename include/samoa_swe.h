@@ -256,8 +256,8 @@ int swe_traverse_graph(swe_ctx* ctx, int64_t n_steps);
  * n_steps = 0 clears it. No reference counterpart. */
 int swe_set_dt_sequence(swe_ctx* ctx, int64_t n_steps, const double* dts);
 
-/* ---- discrete adjoint (single-instance contexts; the f-wave solver and the
- * four Lax-Friedrichs fluxes) ---------------------------------------------- */
+/* ---- discrete adjoint (single-instance contexts; the f-wave and augmented
+ * solvers and the four Lax-Friedrichs fluxes) ------------------------------ */
 /* No reference counterpart: sam(oa)^2 has no adjoint. Cotangent buffers are
  * device pointers with n_cells doubles each. */
 

@@ -1,15 +1,16 @@
-// Discrete adjoint of the SWE step (f-wave solver), hand-written reverse mode.
+// Discrete adjoint of the SWE step (f-wave and augmented solvers, the four
+// Lax-Friedrichs fluxes), hand-written reverse mode.
 //
 // The step x' = F(x, b; dt) is differentiated on the branches its forward
 // evaluation takes (wet/dry fix-ups, wall reconstruction, the Einfeldt
-// min/max, the wave-speed signs that split the net updates, the cell's
-// wetting and drying clamps). dt is frozen (it enters as a constant), so the
-// CFL reduction and the wave speeds' magnitudes are not differentiated.
+// min/max, the wave-speed signs that split the net updates, the augmented
+// solver's Riemann structure, sonic tests and bounds, the LF fluxes' maxima,
+// the cell's wetting and drying clamps). dt is frozen (it enters as a
+// constant), so the CFL reduction is not differentiated.
 //
-// Per edge, fwave_vjp re-evaluates the forward flux of geoclaw_flux<FWAVE>
-// (the same expressions, so the same branches as the forward step) and pulls
-// the cotangents of the two net updates back to (h, hu, hv, b) of both
-// cells. The reverse-step kernel mirrors the forward kernel: a CTA stages a
+// Per edge, geoclaw_vjp / lf_vjp re-evaluate the forward flux (the same
+// expressions, so the same branches as the forward step) and pull the
+// cotangents of the two net updates back to (h, hu, hv, b) of both cells. The reverse-step kernel mirrors the forward kernel: a CTA stages a
 // segment, evaluates each edge task's VJP once and writes each side's result
 // into a per-(cell, local edge) slot in shared memory (no atomics), then each
 // cell sums its slots and its own direct term.
@@ -23,18 +24,425 @@ struct Grad4 {
     double h, hu, hv, b;
 };
 
+// ---------------------------------------------------------------------------
+// Reverse of the augmented solver (riemann_aug_JCP with riemanntype,
+// src/geoclaw/riemannsolvers.f:2-258,507-618). The exact forward (riemann_aug_rec)
+// records its branch decisions; the reverse re-evaluates the values it needs in
+// plain arithmetic under those decisions and pulls the cotangents of the
+// f-waves back to the solver's inputs (the fixed-up depths, momenta,
+// bathymetries, velocities, delphi, the Einfeldt speeds and sqrt(g h)).
+
+// d sqrt(x) / dx times b (0 where the root is 0, as the reference gradient has it)
+__device__ __forceinline__ double dsqrt(double root, double b) { return gt0(root) ? b * 0.5 / root : 0.0; }
+
+// riemanntype's speeds (s1m, s2m) on the recorded branch, and their reverse.
+struct RsCot {
+    double hL, hR, uL, uR, sqL, sqR;
+};
+__device__ __forceinline__ void rs_values(const AugRec& r, double hL, double hR, double uL, double uR, double sqL,
+                                          double sqR, double& s1m, double& s2m) {
+    const double g = kG;
+    const double delu = uR - uL;
+    if (r.rs == 0) {
+        s1m = s2m = ((uR + uL) - 2.0 * sqR) + 2.0 * sqL;
+    } else if (r.rs == 1) {
+        const double t = r.t_pos ? -delu + 2.0 * (sqL + sqR) : 0.0;
+        const double sqm = sqrt(g * ((1.0 / (16.0 * g)) * (t * t)));
+        s1m = (uL + 2.0 * sqL) - 3.0 * sqm;
+        s2m = (uR - 2.0 * sqR) + 3.0 * sqm;
+    } else if (r.rs == 2) {
+        const double h0 = r.highR ? hR : hL;
+        const double gL = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hL)), gR = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hR));
+        const double F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR;
+        const double kk = 4.0 * (h0 * h0);
+        const double dfdh = ((gL - (g * (h0 - hL)) / (kk * gL)) + gR) - (g * (h0 - hR)) / (kk * gR);
+        const double sq0 = sqrt(h0);
+        const double tt = sq0 - F0 / (2.0 * sq0 * dfdh);
+        const double hm = tt * tt;
+        const double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hL));
+        const double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hR));
+        const double sqm = sqrt(g * hm);
+        s1m = u1m - sqm;
+        s2m = u2m + sqm;
+    } else {
+        const double hmn = r.lowR ? hR : hL, hmx = r.highR ? hR : hL;
+        const double sqmn = r.lowR ? sqR : sqL, sqmx = r.highR ? sqR : sqL;
+        const double F0 = delu + 2.0 * (sqmn - sqmx);
+        const double Fmax = delu + (hmx - hmn) * sqrt(((0.5 * g) * (hmx + hmn)) / (hmx * hmn));
+        const double hm = hmn - F0 / ((Fmax - F0) / (hmx - hmn));
+        const double sqm = sqrt(g * hm);
+        if (r.lhigh) {
+            s1m = (uL + 2.0 * sqL) - 3.0 * sqm;
+            s2m = (uL + 2.0 * sqL) - sqm;
+        } else {
+            s2m = (uR - 2.0 * sqR) + 3.0 * sqm;
+            s1m = (uR - 2.0 * sqR) + sqm;
+        }
+    }
+}
+
+__device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, double uL, double uR, double sqL,
+                                       double sqR, double b1, double b2, RsCot& c) {
+    const double g = kG;
+    const double delu = uR - uL;
+    double b_delu = 0.0;
+    if (r.rs == 0) {  // s1m = s2m = ((uR + uL) - 2 sqR) + 2 sqL
+        const double bt = b1 + b2;
+        c.uR += bt;
+        c.uL += bt;
+        c.sqR -= 2.0 * bt;
+        c.sqL += 2.0 * bt;
+        return;
+    }
+    if (r.rs == 1) {  // two rarefactions
+        const double t = r.t_pos ? -delu + 2.0 * (sqL + sqR) : 0.0;
+        const double hm = (1.0 / (16.0 * g)) * (t * t);
+        const double sqm = sqrt(g * hm);
+        c.uL += b1;
+        c.sqL += 2.0 * b1;
+        c.uR += b2;
+        c.sqR -= 2.0 * b2;
+        const double b_sqm = 3.0 * (b2 - b1);
+        const double b_hm = dsqrt(sqm, b_sqm * g);
+        const double b_t = b_hm * t * (1.0 / (8.0 * g));
+        if (r.t_pos) {
+            b_delu -= b_t;
+            c.sqL += 2.0 * b_t;
+            c.sqR += 2.0 * b_t;
+        }
+    } else if (r.rs == 2) {  // two shocks: one Newton step
+        const double h0 = r.highR ? hR : hL;
+        const double i0 = 1.0 / h0, iL = 1.0 / hL, iR = 1.0 / hR;
+        const double gL = sqrt((0.5 * g) * (i0 + iL)), gR = sqrt((0.5 * g) * (i0 + iR));
+        const double F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR;
+        const double kk = 4.0 * (h0 * h0);
+        const double eL = (g * (h0 - hL)) / (kk * gL), eR = (g * (h0 - hR)) / (kk * gR);
+        const double dfdh = ((gL - eL) + gR) - eR;
+        const double sq0 = sqrt(h0);
+        const double slope = 2.0 * sq0 * dfdh;
+        const double tt = sq0 - F0 / slope;
+        const double hm = tt * tt, im = 1.0 / hm;
+        const double cL = sqrt((0.5 * g) * (im + iL)), cR = sqrt((0.5 * g) * (im + iR));
+        const double sqm = sqrt(g * hm);
+        // s1m = u1m - sqm, s2m = u2m + sqm
+        double b_hm = dsqrt(sqm, (b2 - b1) * g);
+        // u2m = uR + (hm - hR) cR, u1m = uL - (hm - hL) cL
+        c.uR += b2;
+        b_hm = fma(b2, cR, b_hm);
+        double b_hR = -b2 * cR;
+        const double b_cR = b2 * (hm - hR);
+        c.uL += b1;
+        b_hm = fma(-b1, cL, b_hm);
+        double b_hL = b1 * cL;
+        const double b_cL = -b1 * (hm - hL);
+        double b_im = 0.0, b_iL = 0.0, b_iR = 0.0, b_i0 = 0.0, b_h0 = 0.0;
+        const double aL = dsqrt(cL, b_cL * (0.5 * g)), aR = dsqrt(cR, b_cR * (0.5 * g));
+        b_im += aL + aR;
+        b_iL += aL;
+        b_iR += aR;
+        b_hm = fma(-b_im, im * im, b_hm);
+        const double b_tt = 2.0 * tt * b_hm;
+        // tt = sq0 - F0 / slope, slope = 2 sq0 dfdh
+        double b_sq0 = b_tt;
+        const double b_F0 = -b_tt / slope;
+        const double b_slope = b_tt * F0 / (slope * slope);
+        b_sq0 = fma(b_slope, 2.0 * dfdh, b_sq0);
+        const double b_dfdh = b_slope * 2.0 * sq0;
+        b_h0 += dsqrt(sq0, b_sq0);
+        // dfdh = ((gL - eL) + gR) - eR
+        double b_gL = b_dfdh, b_gR = b_dfdh;
+        const double b_eL = -b_dfdh, b_eR = -b_dfdh;
+        double b_kk = 0.0;
+        {
+            const double q = g / (kk * gL);
+            b_h0 = fma(b_eL, q, b_h0);
+            b_hL = fma(-b_eL, q, b_hL);
+            b_kk = fma(-b_eL, eL / kk, b_kk);
+            b_gL = fma(-b_eL, eL / gL, b_gL);
+        }
+        {
+            const double q = g / (kk * gR);
+            b_h0 = fma(b_eR, q, b_h0);
+            b_hR = fma(-b_eR, q, b_hR);
+            b_kk = fma(-b_eR, eR / kk, b_kk);
+            b_gR = fma(-b_eR, eR / gR, b_gR);
+        }
+        b_h0 = fma(b_kk, 8.0 * h0, b_h0);
+        // F0 = (delu + (h0 - hL) gL) + (h0 - hR) gR
+        b_delu += b_F0;
+        b_h0 = fma(b_F0, gL + gR, b_h0);
+        b_hL = fma(-b_F0, gL, b_hL);
+        b_hR = fma(-b_F0, gR, b_hR);
+        b_gL = fma(b_F0, h0 - hL, b_gL);
+        b_gR = fma(b_F0, h0 - hR, b_gR);
+        // gL = sqrt(0.5 g (i0 + iL)), gR = sqrt(0.5 g (i0 + iR))
+        const double bgl = dsqrt(gL, b_gL * (0.5 * g)), bgr = dsqrt(gR, b_gR * (0.5 * g));
+        b_i0 += bgl + bgr;
+        b_iL += bgl;
+        b_iR += bgr;
+        b_h0 = fma(-b_i0, i0 * i0, b_h0);
+        b_hL = fma(-b_iL, iL * iL, b_hL);
+        b_hR = fma(-b_iR, iR * iR, b_hR);
+        if (r.highR) b_hR += b_h0;
+        else b_hL += b_h0;
+        c.hL += b_hL;
+        c.hR += b_hR;
+    } else {  // one shock, one rarefaction
+        const double hmn = r.lowR ? hR : hL, hmx = r.highR ? hR : hL;
+        const double sqmn = r.lowR ? sqR : sqL, sqmx = r.highR ? sqR : sqL;
+        const double F0 = delu + 2.0 * (sqmn - sqmx);
+        const double P = ((0.5 * g) * (hmx + hmn)) / (hmx * hmn);
+        const double W = sqrt(P);
+        const double Fmax = delu + (hmx - hmn) * W;
+        const double den = hmx - hmn;
+        const double slope = (Fmax - F0) / den;
+        const double hm = hmn - F0 / slope;
+        const double sqm = sqrt(g * hm);
+        double b_sqm;
+        if (r.lhigh) {
+            const double bb = b1 + b2;
+            c.uL += bb;
+            c.sqL += 2.0 * bb;
+            b_sqm = -3.0 * b1 - b2;
+        } else {
+            const double bb = b1 + b2;
+            c.uR += bb;
+            c.sqR -= 2.0 * bb;
+            b_sqm = 3.0 * b2 + b1;
+        }
+        const double b_hm = dsqrt(sqm, b_sqm * g);
+        // hm = hmn - F0 / slope; slope = (Fmax - F0) / den
+        double b_hmn = b_hm, b_hmx = 0.0;
+        double b_F0 = -b_hm / slope;
+        const double b_slope = b_hm * F0 / (slope * slope);
+        const double b_Fmax = b_slope / den;
+        b_F0 -= b_slope / den;
+        const double b_den = -b_slope * slope / den;
+        b_hmx += b_den;
+        b_hmn -= b_den;
+        // Fmax = delu + (hmx - hmn) W, W = sqrt(P), P = 0.5 g (1 / hmn + 1 / hmx)
+        b_delu += b_Fmax;
+        b_hmx = fma(b_Fmax, W, b_hmx);
+        b_hmn = fma(-b_Fmax, W, b_hmn);
+        const double b_P = dsqrt(W, b_Fmax * (hmx - hmn));
+        b_hmx = fma(-b_P * (0.5 * g), 1.0 / (hmx * hmx), b_hmx);
+        b_hmn = fma(-b_P * (0.5 * g), 1.0 / (hmn * hmn), b_hmn);
+        // F0 = delu + 2 (sq_min - sq_max)
+        b_delu += b_F0;
+        if (r.lowR) c.sqR += 2.0 * b_F0;
+        else c.sqL += 2.0 * b_F0;
+        if (r.highR) c.sqR -= 2.0 * b_F0;
+        else c.sqL -= 2.0 * b_F0;
+        if (r.lowR) c.hR += b_hmn;
+        else c.hL += b_hmn;
+        if (r.highR) c.hR += b_hmx;
+        else c.hL += b_hmx;
+    }
+    c.uR += b_delu;
+    c.uL -= b_delu;
+}
+
+// Cotangents of the augmented solver's inputs.
+struct AugCot {
+    double hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR;
+};
+
+__device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], double hL, double hR, double huL,
+                                        double huR, double bL, double bR, double uL, double uR, double vL, double vR,
+                                        double delphi, double sE1in, double sE2in, double sqL, double sqR,
+                                        AugCot& c) {
+    const double g = kG;
+    // ---- forward values on the recorded branches
+    double s1m, s2m;
+    rs_values(r, hL, hR, uL, uR, sqL, sqR, s1m, s2m);
+    const double delh = hR - hL, delhu = huR - huL, delb = bR - bL;
+    const double l0 = r.l0_sE1 ? sE1in : s2m, l2 = r.l2_sE2 ? sE2in : s1m;
+    const double dsp = l2 - l0;
+    const double q = (((huL - huR) + l2 * hR) - l0 * hL) / dsp;
+    const double hstar = r.hst_pos ? q : 0.0;
+    const double hbar = r.hbar_pos ? 0.5 * (hL + hR) : 0.0;
+    const double su = uL + uR;
+    const double s1s2bar = 0.25 * (su * su) - g * hbar;
+    const double s1s2tilde = (r.tilde_x ? uL * uR : 0.0) - g * hbar;
+    const double dgh = (delb * g) * hbar;
+    const double ddh0 = r.sonic ? -delb : dgh / s1s2bar;
+    const double hsd = hstar * dsp;
+    double hi = 0.0, lo = 0.0;
+    if (r.dcase == 1) {
+        hi = hsd / l2;
+        lo = hsd / l0;
+    } else if (r.dcase == 2) {
+        hi = hsd / l0;
+        lo = -hL;
+    } else if (r.dcase == 3) {
+        hi = hR;
+        lo = hsd / l2;
+    }
+    const double x1 = r.dd_min_first ? ddh0 : hi;
+    const double deldelh = r.dcase ? (r.dd_max_first ? x1 : lo) : ddh0;
+    // (deldelphi and d2 = delphi - deldelphi enter beta1 only, linearly: their values are not needed)
+    const double d0 = delh - deldelh, d1 = delhu;
+    const double det = l0 - l2, id = 1.0 / det;
+    const double beta0 = (d1 - l2 * d0) * id, beta2 = (l0 * d0 - d1) * id;
+    // ---- reverse
+    // fw(3,2) = (((hR uR) vR - (hL uL) vL) - fw(3,1)) - fw(3,3)
+    const double F21 = F[2][1];
+    c.hR = fma(F21, uR * vR, c.hR);
+    c.uR = fma(F21, hR * vR, c.uR);
+    c.vR = fma(F21, hR * uR, c.vR);
+    c.hL = fma(-F21, uL * vL, c.hL);
+    c.uL = fma(-F21, hL * vL, c.uL);
+    c.vL = fma(-F21, hL * uL, c.vL);
+    const double G20 = F[2][0] - F21, G22 = F[2][2] - F21;
+    // fw(1..3, 1) = beta0 (l0, l0^2, l0 vL), fw(2, 2) = beta1, fw(1..3, 3) = beta2 (l2, l2^2, l2 vR)
+    double b_b0 = fma(F[0][0], l0, fma(F[1][0], l0 * l0, G20 * l0 * vL));
+    double b_l0 = fma(F[0][0], beta0, fma(F[1][0], 2.0 * l0 * beta0, G20 * beta0 * vL));
+    c.vL = fma(G20, beta0 * l0, c.vL);
+    const double b_b1 = F[1][1];
+    double b_b2 = fma(F[0][2], l2, fma(F[1][2], l2 * l2, G22 * l2 * vR));
+    double b_l2 = fma(F[0][2], beta2, fma(F[1][2], 2.0 * l2 * beta2, G22 * beta2 * vR));
+    c.vR = fma(G22, beta2 * l2, c.vR);
+    // beta1 = d2 - l0^2 beta0 - l2^2 beta2
+    double b_d2 = b_b1;
+    b_b0 = fma(-b_b1, l0 * l0, b_b0);
+    b_b2 = fma(-b_b1, l2 * l2, b_b2);
+    b_l0 = fma(-b_b1, 2.0 * l0 * beta0, b_l0);
+    b_l2 = fma(-b_b1, 2.0 * l2 * beta2, b_l2);
+    // beta0 = (d1 - l2 d0) / det, beta2 = (l0 d0 - d1) / det, det = l0 - l2
+    double b_d1 = (b_b0 - b_b2) * id;
+    double b_d0 = fma(l0, b_b2, -l2 * b_b0) * id;
+    b_l2 = fma(-d0 * b_b0, id, b_l2);
+    b_l0 = fma(d0 * b_b2, id, b_l0);
+    const double b_det = -fma(b_b0, beta0, b_b2 * beta2) * id;
+    b_l0 += b_det;
+    b_l2 -= b_det;
+    // d0 = delh - deldelh, d1 = delhu, d2 = delphi - deldelphi
+    double b_delh = b_d0, b_delhu = b_d1, b_delb = 0.0;
+    const double b_ddh = -b_d0;
+    c.delphi += b_d2;
+    const double b_ddphi = -b_d2;
+    double b_hbar = 0.0, b_dgh = 0.0, b_sb = 0.0, b_st = 0.0, b_hsd = 0.0;
+    // deldelphi = max(y1, g mn), y1 = min(ddp0, g mx)
+    double b_pl = 0.0, b_pr = 0.0, b_y1 = 0.0, b_ddp0 = 0.0;
+    if (r.ph_max_first) b_y1 = b_ddphi;
+    else if (r.ph_mn_pl) b_pl += g * b_ddphi;
+    else b_pr += g * b_ddphi;
+    if (r.ph_min_first) b_ddp0 = b_y1;
+    else if (r.ph_mx_pl) b_pl += g * b_y1;
+    else b_pr += g * b_y1;
+    // pl = -(hL delb), pr = -(hR delb)
+    c.hL = fma(-b_pl, delb, c.hL);
+    c.hR = fma(-b_pr, delb, c.hR);
+    b_delb = fma(-b_pl, hL, fma(-b_pr, hR, b_delb));
+    if (r.sonic) {  // -((g hbar) delb)
+        b_hbar = fma(-b_ddp0, g * delb, b_hbar);
+        b_delb = fma(-b_ddp0, g * hbar, b_delb);
+    } else {  // -((dgh s1s2tilde) / s1s2bar)
+        b_dgh = fma(-b_ddp0, s1s2tilde / s1s2bar, b_dgh);
+        b_st = fma(-b_ddp0, dgh / s1s2bar, b_st);
+        b_sb = fma(b_ddp0, dgh * s1s2tilde / (s1s2bar * s1s2bar), b_sb);
+    }
+    // deldelh = max(min(ddh0, hi), lo) in the recorded case
+    double b_ddh0 = 0.0;
+    if (r.dcase) {
+        double b_x1 = 0.0, b_lo = 0.0, b_hi = 0.0;
+        if (r.dd_max_first) b_x1 = b_ddh;
+        else b_lo = b_ddh;
+        if (r.dd_min_first) b_ddh0 = b_x1;
+        else b_hi = b_x1;
+        if (r.dcase == 1) {  // hi = hsd / l2, lo = hsd / l0
+            b_hsd = fma(b_hi, 1.0 / l2, fma(b_lo, 1.0 / l0, b_hsd));
+            b_l2 = fma(-b_hi, hsd / (l2 * l2), b_l2);
+            b_l0 = fma(-b_lo, hsd / (l0 * l0), b_l0);
+        } else if (r.dcase == 2) {  // hi = hsd / l0, lo = -hL
+            b_hsd = fma(b_hi, 1.0 / l0, b_hsd);
+            b_l0 = fma(-b_hi, hsd / (l0 * l0), b_l0);
+            c.hL -= b_lo;
+        } else {  // hi = hR, lo = hsd / l2
+            c.hR += b_hi;
+            b_hsd = fma(b_lo, 1.0 / l2, b_hsd);
+            b_l2 = fma(-b_lo, hsd / (l2 * l2), b_l2);
+        }
+    } else {
+        b_ddh0 = b_ddh;
+    }
+    if (r.sonic) {  // -delb
+        b_delb -= b_ddh0;
+    } else {  // dgh / s1s2bar
+        b_dgh = fma(b_ddh0, 1.0 / s1s2bar, b_dgh);
+        b_sb = fma(-b_ddh0, dgh / (s1s2bar * s1s2bar), b_sb);
+    }
+    // hsd = hstar dsp
+    double b_hstar = b_hsd * dsp;
+    double b_dsp = b_hsd * hstar;
+    // dgh = (delb g) hbar
+    b_delb = fma(b_dgh, g * hbar, b_delb);
+    b_hbar = fma(b_dgh, g * delb, b_hbar);
+    // s1s2tilde = max(0, uL uR) - g hbar, s1s2bar = 0.25 su^2 - g hbar, su = uL + uR
+    b_hbar = fma(-(b_st + b_sb), g, b_hbar);
+    if (r.tilde_x) {
+        c.uL = fma(b_st, uR, c.uL);
+        c.uR = fma(b_st, uL, c.uR);
+    }
+    const double b_su = b_sb * 0.5 * su;
+    c.uL += b_su;
+    c.uR += b_su;
+    if (r.hbar_pos) {
+        c.hL += 0.5 * b_hbar;
+        c.hR += 0.5 * b_hbar;
+    }
+    // hstar = max(q, 0), q = (((huL - huR) + l2 hR) - l0 hL) / dsp
+    if (r.hst_pos) {
+        const double bq = b_hstar / dsp;
+        c.huL += bq;
+        c.huR -= bq;
+        b_l2 = fma(bq, hR, b_l2);
+        c.hR = fma(bq, l2, c.hR);
+        b_l0 = fma(-bq, hL, b_l0);
+        c.hL = fma(-bq, l0, c.hL);
+        b_dsp = fma(-bq, q, b_dsp);
+    }
+    // dsp = l2 - l0
+    b_l2 += b_dsp;
+    b_l0 -= b_dsp;
+    // l0 = min(sE1, s2m), l2 = max(sE2, s1m)
+    double b_s1m = 0.0, b_s2m = 0.0;
+    if (r.l0_sE1) c.sE1 += b_l0;
+    else b_s2m += b_l0;
+    if (r.l2_sE2) c.sE2 += b_l2;
+    else b_s1m += b_l2;
+    // delh = hR - hL, delhu = huR - huL, delb = bR - bL
+    c.hR += b_delh;
+    c.hL -= b_delh;
+    c.huR += b_delhu;
+    c.huL -= b_delhu;
+    c.bR += b_delb;
+    c.bL -= b_delb;
+    RsCot rc{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    rs_rev(r, hL, hR, uL, uR, sqL, sqR, b_s1m, b_s2m, rc);
+    c.hL += rc.hL;
+    c.hR += rc.hR;
+    c.uL += rc.uL;
+    c.uR += rc.uR;
+    c.sqL += rc.sqL;
+    c.sqR += rc.sqR;
+}
+
 // VJP of the f-wave edge flux: given the cotangents gL / gR of the left/right
 // net updates (h, hu, hv, world frame), add the cotangents of the inputs to
 // outL / outR. QL / QR are the states (h = surface), dL / dR their depths,
 // sqL0 / sqR0 their sqrt(g * depth) as in the forward step.
 // axis: the normal's direction as in geoclaw_flux (0 diagonal, 1 along x, 2 along y).
-__device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL, const State& QR, double dL0,
-                                       double dR0, double sqL0, double sqR0, double yL0, double yR0, double drytol,
-                                       const double gL[3], const double gR[3], Grad4& outL, Grad4& outR,
-                                       int axis = 0) {
+// SOLVER: FWAVE or AUG_RIEMANN (the solver core between the shared wet/dry
+// handling, Einfeldt speeds and net-update split of c_bind_geoclaw_solver_dp).
+template <int SOLVER>
+__device__ __forceinline__ void geoclaw_vjp(double n1, double n2, const State& QL, const State& QR, double dL0,
+                                            double dR0, double sqL0, double sqR0, double yL0, double yR0,
+                                            double drytol, const double gL[3], const double gR[3], Grad4& outL,
+                                            Grad4& outR, int axis = 0) {
     const double g = kG;
     const double c = 0.5 * g;
-    // ---------------- forward (geoclaw_flux<FWAVE>, the same values)
+    // ---------------- forward (geoclaw_flux<SOLVER>, the same values)
     const bool fin = is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
     const bool fast = axis != 0 && fin;
     const bool sn = axis == 1 ? lt0(n1) : lt0(n2);
@@ -115,13 +523,26 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
     const double delphi = ((((huR - huL) * (uL + uR)) - ((uL * uR) * (hR - hL))) + ((c * X) * Hs)) - ((c * Hs) * dB);
     const double delhu = huR - huL;
     const double K = (g * 0.5) * Hs;
-    const double ddp = -(K * dB);
-    const double dpd = delphi - ddp;
-    const double D = sE2 - sE1;
-    const Recip rD = recip_rn(D);
-    const double beta1 = div_rn(sE2 * delhu - dpd, rD);
-    const double beta2 = div_rn(dpd - sE1 * delhu, rD);
-    const double sw[3] = {sE1, 0.5 * (sE1 + sE2), sE2};
+    double beta1 = 0.0, beta2 = 0.0, sw[3];
+    Recip rD{1.0, 1.0, false};
+    AugRec rec{};
+    if (SOLVER == FWAVE) {
+        const double ddp = -(K * dB);
+        const double dpd = delphi - ddp;
+        const double D = sE2 - sE1;
+        rD = recip_rn(D);
+        beta1 = div_rn(sE2 * delhu - dpd, rD);
+        beta2 = div_rn(dpd - sE1 * delhu, rD);
+        sw[0] = sE1;
+        sw[1] = 0.5 * (sE1 + sE2);
+        sw[2] = sE2;
+    } else {  // the same call as geoclaw_solver's, recording the branch decisions
+        const double yLf = wall_l ? yR0 : yL0, yRf = wall_r ? yL0 : yR0;
+        const bool okL = (wetL || wall_l) && recip_fast(hL), okR = (wetR || wall_r) && recip_fast(hR);
+        double fwa[3][3];
+        riemann_aug_rec<true>(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR, yLf, yRf, okL,
+                              okR, drytol, sw, fwa, &rec);
+    }
     // ---------------- reverse (cotangents: products fused into FMAs where they feed a sum; they
     // need no bit-exact agreement, only the forward recompute above does)
     // back-rotation p = net(2:3) T (for an axis-aligned normal: signed selections)
@@ -150,38 +571,68 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
             F[e][w] = zeroed ? 0.0 : f;
         }
     }
-    // fw(3,2) = ((huR vR - huL vL) - fw(3,1)) - fw(3,3); wave 2 carries no h / hu
-    double b_huR = F[2][1] * vR, b_vR = F[2][1] * huR, b_huL = -F[2][1] * vL, b_vL = -F[2][1] * huL;
-    const double F30 = F[2][0] - F[2][1], F32 = F[2][2] - F[2][1];
-    double b_beta1 = fma(F30, vL, fma(F[1][0], sE1, F[0][0]));
-    double b_beta2 = fma(F32, vR, fma(F[1][2], sE2, F[0][2]));
-    double b_sE1 = F[1][0] * beta1, b_sE2 = F[1][2] * beta2;
-    b_vL = fma(F30, beta1, b_vL);
-    b_vR = fma(F32, beta2, b_vR);
-    // beta1 = (sE2 delhu - dpd) / D, beta2 = (dpd - sE1 delhu) / D, D = sE2 - sE1
-    const double N1b = b_beta1 * rD.y, N2b = b_beta2 * rD.y;
-    const double b_D = -fma(b_beta1, beta1, b_beta2 * beta2) * rD.y;
-    b_sE2 += fma(N1b, delhu, b_D);
-    b_sE1 -= fma(N2b, delhu, b_D);
-    double b_delhu = fma(N1b, sE2, -(N2b * sE1));
-    const double b_dpd = N2b - N1b;
-    // dpd = delphi - ddp, ddp = -(K dB), K = c Hs
-    double b_delphi = b_dpd;
-    const double b_ddp = -b_dpd;
-    double b_K = -b_ddp * dB;
-    double b_dB = -b_ddp * K;
-    double b_Hs = b_K * c;
-    // delhu = huR - huL
-    b_huR += b_delhu;
-    b_huL -= b_delhu;
+    double b_huR, b_vR, b_huL, b_vL, b_sE1, b_sE2, b_delphi, b_dB, b_Hs;
+    // the solver core's cotangents of hL, hR, bL, bR, uL, uR, sqrt(g h) (the f-wave has
+    // them through delphi, K and the Einfeldt speeds only)
+    double k_hL = 0.0, k_hR = 0.0, k_bL = 0.0, k_bR = 0.0, k_uL = 0.0, k_uR = 0.0, k_sqL = 0.0, k_sqR = 0.0;
+    if (SOLVER == FWAVE) {
+        // fw(3,2) = ((huR vR - huL vL) - fw(3,1)) - fw(3,3); wave 2 carries no h / hu
+        b_huR = F[2][1] * vR;
+        b_vR = F[2][1] * huR;
+        b_huL = -F[2][1] * vL;
+        b_vL = -F[2][1] * huL;
+        const double F30 = F[2][0] - F[2][1], F32 = F[2][2] - F[2][1];
+        double b_beta1 = fma(F30, vL, fma(F[1][0], sE1, F[0][0]));
+        double b_beta2 = fma(F32, vR, fma(F[1][2], sE2, F[0][2]));
+        b_sE1 = F[1][0] * beta1;
+        b_sE2 = F[1][2] * beta2;
+        b_vL = fma(F30, beta1, b_vL);
+        b_vR = fma(F32, beta2, b_vR);
+        // beta1 = (sE2 delhu - dpd) / D, beta2 = (dpd - sE1 delhu) / D, D = sE2 - sE1
+        const double N1b = b_beta1 * rD.y, N2b = b_beta2 * rD.y;
+        const double b_D = -fma(b_beta1, beta1, b_beta2 * beta2) * rD.y;
+        b_sE2 += fma(N1b, delhu, b_D);
+        b_sE1 -= fma(N2b, delhu, b_D);
+        double b_delhu = fma(N1b, sE2, -(N2b * sE1));
+        const double b_dpd = N2b - N1b;
+        // dpd = delphi - ddp, ddp = -(K dB), K = c Hs
+        b_delphi = b_dpd;
+        const double b_ddp = -b_dpd;
+        double b_K = -b_ddp * dB;
+        b_dB = -b_ddp * K;
+        b_Hs = b_K * c;
+        // delhu = huR - huL
+        b_huR += b_delhu;
+        b_huL -= b_delhu;
+    } else {
+        AugCot ac{};
+        aug_rev(rec, F, hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR, ac);
+        b_huR = ac.huR;
+        b_huL = ac.huL;
+        b_vR = ac.vR;
+        b_vL = ac.vL;
+        b_sE1 = ac.sE1;
+        b_sE2 = ac.sE2;
+        b_delphi = ac.delphi;
+        b_dB = 0.0;
+        b_Hs = 0.0;
+        k_hL = ac.hL;
+        k_hR = ac.hR;
+        k_bL = ac.bL;
+        k_bR = ac.bR;
+        k_uL = ac.uL;
+        k_uR = ac.uR;
+        k_sqL = ac.sqL;
+        k_sqR = ac.sqR;
+    }
     // Einfeldt speeds
     double b_sL = e1_is_sL ? b_sE1 : 0.0, b_r1 = e1_is_sL ? 0.0 : b_sE1;
     double b_sR = e2_is_sR ? b_sE2 : 0.0, b_r2 = e2_is_sR ? 0.0 : b_sE2;
     const double b_uhat = b_r1 + b_r2;
     const double b_chat = b_r2 - b_r1;
     if (chat > 0.0) b_Hs = fma(b_chat * (0.5 * rcp_nr(chat)), g * 0.5, b_Hs);
-    double b_uL = b_sL, b_uR = b_sR;
-    double b_sqL = -b_sL, b_sqR = b_sR;
+    double b_uL = b_sL + k_uL, b_uR = b_sR + k_uR;
+    double b_sqL = k_sqL - b_sL, b_sqR = b_sR + k_sqR;
     const double b_A = b_uhat * rB.y, b_B = -b_uhat * uhat * rB.y;
     b_sqL += fma(b_A, uL, b_B);
     b_sqR += fma(b_A, uR, b_B);
@@ -196,12 +647,12 @@ __device__ __forceinline__ void fwave_vjp(double n1, double n2, const State& QL,
         b_huL -= dsu;
         b_uL += fma(d, dhu, -(d * uR * dh));
         b_uR += fma(d, dhu, -(d * uL * dh));
-        double b_hR = -d * uu, b_hL = d * uu;
+        double b_hR = fma(-d, uu, k_hR), b_hL = fma(d, uu, k_hL);
         const double b_X = d * c * Hs;
         b_Hs += fma(d, c * X, -(d * c * dB));
         b_dB = fma(-d, c * Hs, b_dB);
         // X = ((bR + hR) - bL) - hL
-        double b_bR = b_X, b_bL = -b_X;
+        double b_bR = b_X + k_bR, b_bL = k_bL - b_X;
         b_hR += b_X;
         b_hL -= b_X;
         // Hs = hR + hL, dB = bR - bL
@@ -468,8 +919,10 @@ template <int SOLVER>
 __device__ __forceinline__ void edge_vjp(double n1, double n2, const State& QL, const State& QR, double dL,
                                          double dR, double sqL, double sqR, double yL, double yR, double drytol,
                                          const double gL[3], const double gR[3], Grad4& oL, Grad4& oR, int axis) {
-    if (SOLVER == FWAVE) fwave_vjp(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, gL, gR, oL, oR, axis);
-    else lf_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, gL, gR, oL, oR);
+    if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
+        geoclaw_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, gL, gR, oL, oR, axis);
+    else
+        lf_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, gL, gR, oL, oR);
 }
 
 template <int SOLVER>

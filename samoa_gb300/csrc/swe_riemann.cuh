@@ -261,20 +261,40 @@ __device__ __forceinline__ double iabs(double x) { return bitsd(abs_bits(x)); } 
 // rounded (recip_rn's fast range), else the IEEE division.
 __device__ __forceinline__ double inv_of(double h, double y, bool y_ok) { return y_ok ? y : 1.0 / h; }
 
+// The branch decisions of one augmented-solver evaluation, for its reverse
+// (the discrete adjoint re-evaluates the values; the decisions fix the branch).
+struct AugRec {
+    int8_t rs;        // riemanntype: 0 a side at most dry, 1 two rarefactions, 2 two shocks, 3 one of each
+    bool lowR, highR;  // h_min resp. h_max is hR
+    bool lhigh;        // one of each: hL > hR
+    bool t_pos;        // two rarefactions: t = -delu + 2 (sqL + sqR) kept (not the 0)
+    bool l0_sE1, l2_sE2, hst_pos, hbar_pos, tilde_x, sonic;
+    int8_t dcase;      // deldelh bounds: 0 none, 1 both speeds apart, 2 sE1 >= ct, 3 sE2 <= -ct
+    bool dd_min_first, dd_max_first;  // each bound kept the running value
+    bool ph_mx_pl, ph_min_first, ph_mn_pl, ph_max_first;  // deldelphi bounds
+};
+
 // Riemann structure with one Newton step, src/geoclaw/riemannsolvers.f:507-618.
 // sqL / sqR are sqrt(g * hL) and sqrt(g * hR) (the caller's, the same operands
 // and so the same bits as computing them here); yL / yR are RN(1 / hL) and
 // RN(1 / hR) where yL_ok / yR_ok, else the divisions are done here.
-__device__ __forceinline__ void riemann_structure_core(double hL, double hR, double uL, double uR, double drytol,
-                                                      double sqL, double sqR, double yL, double yR, bool yL_ok,
-                                                      bool yR_ok, double& hm, double& s1m, double& s2m) {
+template <bool REC>
+__device__ __forceinline__ void riemann_structure_rec(double hL, double hR, double uL, double uR, double drytol,
+                                                     double sqL, double sqR, double yL, double yR, bool yL_ok,
+                                                     bool yR_ok, double& hm, double& s1m, double& s2m,
+                                                     AugRec* rec) {
     const double g = kG;
     const bool r_lower = lt(hR, hL);  // h_min = dmn(hR, hL) is hR
     const double h_min = r_lower ? hR : hL, sq_min = r_lower ? sqR : sqL;
     const bool r_higher = lt(hL, hR);  // h_max = dmx(hR, hL) is hR
     const double h_max = r_higher ? hR : hL, sq_max = r_higher ? sqR : sqL;
+    if (REC) {
+        rec->lowR = r_lower;
+        rec->highR = r_higher;
+    }
     double delu = uR - uL;
     if (le(h_min, drytol)) {
+        if (REC) rec->rs = 0;
         hm = 0.0;
         double t = ((uR + uL) - scale_pow2(sqR, 1, 2.0)) + scale_pow2(sqL, 1, 2.0);
         s1m = t;
@@ -284,12 +304,18 @@ __device__ __forceinline__ void riemann_structure_core(double hL, double hR, dou
     double F_min = delu + scale_pow2(sq_min - sq_max, 1, 2.0);
     double F_max = delu + (h_max - h_min) * sqrt(((0.5 * g) * (h_max + h_min)) / (h_max * h_min));
     if (gt0(F_min)) {  // two rarefactions
-        double t = imax(0.0, -delu + scale_pow2(sqL + sqR, 1, 2.0));
+        const double t0 = -delu + scale_pow2(sqL + sqR, 1, 2.0);
+        double t = imax(0.0, t0);
+        if (REC) {
+            rec->rs = 1;
+            rec->t_pos = !lt(t0, 0.0);
+        }
         hm = (1.0 / (16.0 * g)) * (t * t);
         const double sqm = sqrt(g * hm);
         s1m = (uL + scale_pow2(sqL, 1, 2.0)) - 3.0 * sqm;
         s2m = (uR - scale_pow2(sqR, 1, 2.0)) + 3.0 * sqm;
     } else if (le(F_max, 0.0)) {  // two shocks: one Newton step on sqrt(h)
+        if (REC) rec->rs = 2;
         double h0 = h_max;
         const double i0 = r_higher ? inv_of(hR, yR, yR_ok) : inv_of(hL, yL, yL_ok);
         const double iL = inv_of(hL, yL, yL_ok), iR = inv_of(hR, yR, yR_ok);
@@ -309,6 +335,10 @@ __device__ __forceinline__ void riemann_structure_core(double hL, double hR, dou
         s1m = u1m - sqm;
         s2m = u2m + sqm;
     } else {  // one shock, one rarefaction
+        if (REC) {
+            rec->rs = 3;
+            rec->lhigh = lt(hR, hL);
+        }
         double h0 = h_min;
         const double i0 = r_lower ? inv_of(hR, yR, yR_ok) : inv_of(hL, yL, yL_ok);
         double F0 = (delu + scale_pow2(sq_min - sq_max, 1, 2.0)) + (h0 - h_min) * sqrt((0.5 * g) * (i0 + i0));
@@ -323,6 +353,12 @@ __device__ __forceinline__ void riemann_structure_core(double hL, double hR, dou
             s1m = (uR - scale_pow2(sqR, 1, 2.0)) + sqm;
         }
     }
+}
+
+__device__ __forceinline__ void riemann_structure_core(double hL, double hR, double uL, double uR, double drytol,
+                                                      double sqL, double sqR, double yL, double yR, bool yL_ok,
+                                                      bool yR_ok, double& hm, double& s1m, double& s2m) {
+    riemann_structure_rec<false>(hL, hR, uL, uR, drytol, sqL, sqR, yL, yR, yL_ok, yR_ok, hm, s1m, s2m, nullptr);
 }
 
 // The same with sqrt(g * h) and the reciprocals computed here (the wet/dry
@@ -364,36 +400,44 @@ __device__ __forceinline__ bool moderate(double x) { return abs_bits(x) < 0x52b0
 // f-waves, whose zeros the net-update accumulation turns into +0, except as a
 // divisor: a zero determinant, and operands that are not finite or so large
 // that a product could overflow, take the source's full expressions.
-static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
-                                                double uL, double uR, double vL, double vR, double delphi,
-                                                double sE1, double sE2, double sqL, double sqR, double yL,
-                                                double yR, bool yL_ok, bool yR_ok, double drytol, double sw[3],
-                                                double fw[3][3]) {
+template <bool REC>
+__device__ __forceinline__ void riemann_aug_rec(double hL, double hR, double huL, double huR, double bL, double bR,
+                                               double uL, double uR, double vL, double vR, double delphi,
+                                               double sE1, double sE2, double sqL, double sqR, double yL,
+                                               double yR, bool yL_ok, bool yR_ok, double drytol, double sw[3],
+                                               double fw[3][3], AugRec* rec) {
     const double g = kG;
     double delh = hR - hL;
     double delhu = huR - huL;
     double delb = bR - bL;
     double hm, s1m, s2m;
-    riemann_structure_core(hL, hR, uL, uR, drytol, sqL, sqR, yL, yR, yL_ok, yR_ok, hm, s1m, s2m);
+    riemann_structure_rec<REC>(hL, hR, uL, uR, drytol, sqL, sqR, yL, yR, yL_ok, yR_ok, hm, s1m, s2m, rec);
     double l0 = imin(sE1, s2m);
     double l2 = imax(sE2, s1m);
+    if (REC) {
+        rec->l0_sE1 = lt(sE1, s2m);
+        rec->l2_sE2 = lt(s1m, sE2);
+    }
     sE1 = l0;
     sE2 = l2;
     // sE2 - sE1 = -(l0 - l2) exactly (round to nearest is symmetric): one
     // reciprocal serves hstarHLL's divisor and the Cramer determinant
     const double dsp = sE2 - sE1;
     const Recip rsp = recip_rn(dsp);
-    double hstarHLL = imax(div_rn(((huL - huR) + sE2 * hR) - sE1 * hL, rsp), 0.0);
+    const double hq = div_rn(((huL - huR) + sE2 * hR) - sE1 * hL, rsp);
+    double hstarHLL = imax(hq, 0.0);
     double l1 = scale_pow2(l0 + l2, -1, 0.5);
     if (lt(iabs(l1), 1e-20)) l1 = 0.0;
     const double r20 = l0 * l0, r22 = l2 * l2;
 
     const double ct = 1e-6;
-    double hbar = imax(scale_pow2(hL + hR, -1, 0.5), 0.0);
+    const double hhalf = scale_pow2(hL + hR, -1, 0.5);
+    double hbar = imax(hhalf, 0.0);
     double su = uL + uR;
     const double ghbar = g * hbar;
     double s1s2bar = scale_pow2(su * su, -2, 0.25) - ghbar;
-    double s1s2tilde = imax(0.0, uL * uR) - ghbar;
+    const double uLR = uL * uR;
+    double s1s2tilde = imax(0.0, uLR) - ghbar;
     bool sonic = le(iabs(s1s2bar), ct);
     sonic |= le(s1s2bar * s1s2tilde, ct);
     sonic |= le((s1s2bar * sE1) * sE2, ct);
@@ -402,6 +446,13 @@ static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL
     sonic |= gt0(sE2) && lt0(s2m);
     sonic |= lt0((uL + sqL) * (uR + sqR));  // sqrt(g * h) of the fixed-up depths
     sonic |= lt0((uL - sqL) * (uR - sqR));
+    if (REC) {
+        rec->hst_pos = lt(0.0, hq);
+        rec->hbar_pos = lt(0.0, hhalf);
+        rec->tilde_x = !lt(uLR, 0.0);
+        rec->sonic = sonic;
+        rec->dcase = 0;
+    }
 
     double deldelh, deldelphi;
     const double dgh = (delb * g) * hbar;
@@ -414,19 +465,40 @@ static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL
         deldelphi = flip(div_rn(dgh * s1s2tilde, rb), true);
     }
     const double hsd = hstarHLL * dsp;
+    int dcase = 0;
+    double lo = 0.0, hi = 0.0;  // the two bounds of the case
     if (lt(sE1, -ct) && lt(ct, sE2)) {
-        deldelh = imin(deldelh, hsd / sE2);
-        deldelh = imax(deldelh, hsd / sE1);
+        dcase = 1;
+        hi = hsd / sE2;
+        lo = hsd / sE1;
     } else if (le(ct, sE1)) {
-        deldelh = imin(deldelh, hsd / sE1);
-        deldelh = imax(deldelh, flip(hL, true));
+        dcase = 2;
+        hi = hsd / sE1;
+        lo = flip(hL, true);
     } else if (le(sE2, -ct)) {
-        deldelh = imin(deldelh, hR);
-        deldelh = imax(deldelh, hsd / sE2);
+        dcase = 3;
+        hi = hR;
+        lo = hsd / sE2;
+    }
+    if (dcase) {
+        const double x1 = imin(deldelh, hi);
+        if (REC) {
+            rec->dcase = (int8_t)dcase;
+            rec->dd_min_first = lt(deldelh, hi);
+            rec->dd_max_first = lt(lo, x1);
+        }
+        deldelh = imax(x1, lo);
     }
     const double pl = flip(hL * delb, true), pr = flip(hR * delb, true);
-    deldelphi = imin(deldelphi, g * imax(pl, pr));
-    deldelphi = imax(deldelphi, g * imin(pl, pr));
+    const double gmx = g * imax(pl, pr), gmn = g * imin(pl, pr);
+    const double y1 = imin(deldelphi, gmx);
+    if (REC) {
+        rec->ph_mx_pl = lt(pr, pl);
+        rec->ph_min_first = lt(deldelphi, gmx);
+        rec->ph_mn_pl = lt(pl, pr);
+        rec->ph_max_first = lt(gmn, y1);
+    }
+    deldelphi = imax(y1, gmn);
     double d0 = delh - deldelh, d1 = delhu, d2 = delphi - deldelphi;
 
     double beta0, beta1, beta2;
@@ -456,6 +528,15 @@ static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL
     fw[0][1] = mul0(beta1); fw[1][1] = beta1;
     fw[0][2] = beta2 * l2; fw[1][2] = beta2 * r22; fw[2][2] = (beta2 * l2) * vR;
     fw[2][1] = ((((hR * uR) * vR) - ((hL * uL) * vL)) - fw[2][0]) - fw[2][2];
+}
+
+static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL, double huR, double bL, double bR,
+                                                double uL, double uR, double vL, double vR, double delphi,
+                                                double sE1, double sE2, double sqL, double sqR, double yL,
+                                                double yR, bool yL_ok, bool yR_ok, double drytol, double sw[3],
+                                                double fw[3][3]) {
+    riemann_aug_rec<false>(hL, hR, huL, huR, bL, bR, uL, uR, vL, vR, delphi, sE1, sE2, sqL, sqR, yL, yR, yL_ok,
+                           yR_ok, drytol, sw, fw, nullptr);
 }
 
 // Wet/dry handling, wave speeds and net updates of c_bind_geoclaw_solver_dp

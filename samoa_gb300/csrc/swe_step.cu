@@ -1151,6 +1151,7 @@ typedef void (*AdjKernel)(AdjointArgs);
 AdjKernel adjoint_kernel_for(int solver) {
     switch (solver) {
         case FWAVE: return adjoint_kernel<FWAVE>;
+        case AUG_RIEMANN: return adjoint_kernel<AUG_RIEMANN>;
         case LF: return adjoint_kernel<LF>;
         case LF_BATH: return adjoint_kernel<LF_BATH>;
         case LLF: return adjoint_kernel<LLF>;
@@ -1194,7 +1195,7 @@ int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double*
     const size_t smem = (size_t)21 * c->seg_cells * sizeof(double);
     const int solver = c->params[0].solver;
     const AdjKernel kern = adjoint_kernel_for(solver);
-    if (!kern) return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave and Lax-Friedrichs fluxes");
+    if (!kern) return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave, augmented and Lax-Friedrichs fluxes");
     if (c->adj_seg_cells != c->seg_cells || c->adj_solver != solver) {
         CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
@@ -1218,7 +1219,7 @@ int swe_adjoint_step(swe_ctx* c, const uint8_t* branch, const double* lam_h, con
     if (rc) return rc;
     if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
     if (!adjoint_kernel_for(c->params[0].solver))
-        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave and Lax-Friedrichs fluxes");
+        return set_error(SWE_E_INVALID, "the adjoint step differentiates the f-wave, augmented and Lax-Friedrichs fluxes");
     if (!lam_h || !lam_hu || !lam_hv || !out_h || !out_hu || !out_hv || !bbar)
         return set_error(SWE_E_INVALID, "null cotangent buffer");
     cudaSetDevice(c->device);
@@ -1528,7 +1529,7 @@ int swe_gauge_gradient(swe_ctx* c, int64_t n_steps, const double* dts, int32_t s
     if (rc) return rc;
     if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "the adjoint runs on single-instance contexts");
     if (!adjoint_kernel_for(c->params[0].solver))
-        return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave and Lax-Friedrichs fluxes");
+        return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave, augmented and Lax-Friedrichs fluxes");
     if (n_steps < 1 || !dts || snapshots < 1 || n_gauges < 1 || !gauges || !obs || !grad_h || !grad_b || !J)
         return set_error(SWE_E_INVALID, "bad arguments");
     cudaSetDevice(c->device);

@@ -43,3 +43,22 @@ def assert_state_equal(tag, h, hu, hv, ref_h, ref_hu, ref_hv):
 def rel_l2(a, b):
     den = max(float(np.linalg.norm(b)), 1e-300)
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b))) / den
+
+
+def random_states_scenario(solver, seed=5, depth=9):
+    """Random wet states on a uniform mesh: shocks, rarefactions and mixed waves on
+    every edge kind (every branch of the augmented solver's riemanntype), about
+    5 % dry cells, outflow walls."""
+    from samoa_gb300 import scenarios, swe
+    mesh = swe.uniform_mesh(depth)
+    n = mesh.n_cells
+    rng = np.random.default_rng(seed)
+    b = rng.uniform(-12.0, -2.0, n)
+    d = rng.uniform(0.5, 10.0, n) * (rng.random(n) > 0.05)
+    h = b + d
+    hu = rng.normal(0.0, 6.0, n) * d
+    hv = rng.normal(0.0, 6.0, n) * d
+    cfg = swe.Config(flux_solver=solver, boundary="outflow", courant_number=0.3, dry_tolerance=1e-3, scaling=1.0,
+                     offset=(-0.5, -0.5), i_min_depth=depth - 1, i_max_depth=depth + 1)
+    dt = swe.initial_dt(mesh, h, hu, hv, b, cfg.courant_number)
+    return scenarios.Scenario("random", swe.Grid(mesh, h, hu, hv, b, 0.0, dt), cfg, 4)

@@ -1,5 +1,6 @@
-"""GPU discrete adjoint of the f-wave step: one-step VJP against torch
-autograd of the FP64 restatement, the checkpointed multi-step gauge gradient
+"""GPU discrete adjoint of the step (f-wave, augmented and Lax-Friedrichs
+fluxes): one-step VJP against torch autograd of the FP64 restatement, the
+checkpointed multi-step gauge gradient
 against the FP64 CPU adjoint, and the gradient against central finite
 differences (frozen dt sequence)."""
 import ctypes as C
@@ -9,6 +10,8 @@ import pytest
 
 from oracle import swe_torch as ST
 from samoa_gb300 import _lib, adjoint, scenarios, swe
+
+from .helpers import random_states_scenario
 
 pytestmark = pytest.mark.gpu
 
@@ -27,14 +30,18 @@ def _prep(scn, warm_steps):
 
 
 CASES = [("bowl_outflow", "fwave"), ("bowl_noslip", "fwave"), ("dam_slip", "fwave"), ("dam_outflow", "fwave"),
-         ("bowl_outflow", "llfbath"), ("bowl_noslip", "lfbath"), ("dam_slip", "lf"), ("dam_outflow", "llf")]
+         ("bowl_outflow", "llfbath"), ("bowl_noslip", "lfbath"), ("dam_slip", "lf"), ("dam_outflow", "llf"),
+         ("bowl_outflow", "aug_riemann"), ("bowl_noslip", "aug_riemann"), ("dam_slip", "aug_riemann"),
+         ("random", "aug_riemann"), ("random", "fwave"), ("random", "llfbath")]
 
 
 @pytest.mark.parametrize("case,solver", CASES)
 @pytest.mark.parametrize("parity", [0, 1])
 def test_adjoint_step_matches_torch_vjp(swe_lib, case, solver, parity):
     import torch
-    if case.startswith("bowl"):
+    if case == "random":
+        scn = random_states_scenario(solver)
+    elif case.startswith("bowl"):
         scn = scenarios.parabolic_bowl(log2_cells=10, solver=solver, amplitude=2.5, sigma=0.08)
         scn.cfg.boundary = "noslip" if case.endswith("noslip") else "outflow"
     else:
@@ -88,11 +95,12 @@ def test_adjoint_step_matches_torch_vjp(swe_lib, case, solver, parity):
         assert err < 1e-11, (case, solver, parity, name, err)
 
 
-def test_gauge_gradient_matches_cpu_adjoint(swe_lib):
+@pytest.mark.parametrize("solver", ["fwave", "aug_riemann", "llfbath"])
+def test_gauge_gradient_matches_cpu_adjoint(swe_lib, solver):
     """J over 40 steps with wet/dry fronts, 3 snapshot slots (forces recomputation):
     GPU checkpointed adjoint against torch autograd of the FP64 restatement."""
     import torch
-    scn = scenarios.parabolic_bowl(log2_cells=10, solver="fwave", amplitude=2.5, sigma=0.08)
+    scn = scenarios.parabolic_bowl(log2_cells=10, solver=solver, amplitude=2.5, sigma=0.08)
     mesh, cfg = scn.grid.mesh, scn.cfg
     params = cfg.params()
     h0, b = scn.grid.h.copy(), scn.grid.b.copy()
@@ -106,14 +114,14 @@ def test_gauge_gradient_matches_cpu_adjoint(swe_lib):
         J, gh, gbar = P.gradient(h0, b)
     finally:
         P.close()
-    T = ST.TorchStep(mesh, scaling=cfg.scaling, drytol=cfg.dry_tolerance, bc=cfg.boundary)
+    T = ST.TorchStep(mesh, scaling=cfg.scaling, drytol=cfg.dry_tolerance, bc=cfg.boundary, solver=solver)
     z = torch.zeros(mesh.n_cells, dtype=torch.float64)
     Jr, ghr, gbr = ST.gauge_objective_and_grad(T, torch.tensor(h0), z, z, torch.tensor(b), dts,
                                                torch.tensor(gauges), torch.tensor(obs))
     assert abs(J - Jr) <= 1e-12 * abs(Jr)
     for g_, r_ in ((gh.cpu().numpy(), ghr.numpy()), (gbar.cpu().numpy(), gbr.numpy())):
         err = np.abs(g_ - r_).max() / np.abs(r_).max()
-        assert err < 1e-9, err
+        assert err < 1e-9, (solver, err)
 
 
 def test_gradient_matches_central_differences_h0(swe_lib):

@@ -7,30 +7,12 @@ import pytest
 from oracle import swe_torch as ST
 from samoa_gb300 import scenarios
 
-from .helpers import omp_state, oracle_params
-
-
-def _random_case(solver, seed=5):
-    """Random wet states on a uniform mesh: shocks, rarefactions and mixed waves
-    on every edge kind (every branch of riemanntype), some dry cells."""
-    from samoa_gb300 import swe
-    mesh = swe.uniform_mesh(9)
-    n = mesh.n_cells
-    rng = np.random.default_rng(seed)
-    b = rng.uniform(-12.0, -2.0, n)
-    depth = rng.uniform(0.5, 10.0, n) * (rng.random(n) > 0.05)
-    h = b + depth
-    hu = rng.normal(0.0, 6.0, n) * depth
-    hv = rng.normal(0.0, 6.0, n) * depth
-    cfg = swe.Config(flux_solver=solver, boundary="outflow", courant_number=0.3, dry_tolerance=1e-3, scaling=1.0,
-                     offset=(-0.5, -0.5), i_min_depth=8, i_max_depth=10)
-    dt = swe.initial_dt(mesh, h, hu, hv, b, cfg.courant_number)
-    return scenarios.Scenario("random", swe.Grid(mesh, h, hu, hv, b, 0.0, dt), cfg, 4)
+from .helpers import omp_state, oracle_params, random_states_scenario
 
 
 def _case(name, solver):
     if name == "random":
-        scn = _random_case(solver)
+        scn = random_states_scenario(solver)
     elif name == "bowl":
         scn = scenarios.parabolic_bowl(log2_cells=10, solver=solver, amplitude=2.5, sigma=0.08)
     else:
