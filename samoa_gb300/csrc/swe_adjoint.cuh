@@ -35,50 +35,13 @@ struct Grad4 {
 // d sqrt(x) / dx times b (0 where the root is 0, as the reference gradient has it)
 __device__ __forceinline__ double dsqrt(double root, double b) { return gt0(root) ? b * 0.5 / root : 0.0; }
 
-// riemanntype's speeds (s1m, s2m) on the recorded branch, and their reverse.
+// Cotangents of riemanntype's inputs.
 struct RsCot {
     double hL, hR, uL, uR, sqL, sqR;
 };
-__device__ __forceinline__ void rs_values(const AugRec& r, double hL, double hR, double uL, double uR, double sqL,
-                                          double sqR, double& s1m, double& s2m) {
-    const double g = kG;
-    const double delu = uR - uL;
-    if (r.rs == 0) {
-        s1m = s2m = ((uR + uL) - 2.0 * sqR) + 2.0 * sqL;
-    } else if (r.rs == 1) {
-        const double t = r.t_pos ? -delu + 2.0 * (sqL + sqR) : 0.0;
-        const double sqm = sqrt(g * ((1.0 / (16.0 * g)) * (t * t)));
-        s1m = (uL + 2.0 * sqL) - 3.0 * sqm;
-        s2m = (uR - 2.0 * sqR) + 3.0 * sqm;
-    } else if (r.rs == 2) {
-        const double h0 = r.highR ? hR : hL;
-        const double gL = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hL)), gR = sqrt((0.5 * g) * (1.0 / h0 + 1.0 / hR));
-        const double F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR;
-        const double kk = 4.0 * (h0 * h0);
-        const double dfdh = ((gL - (g * (h0 - hL)) / (kk * gL)) + gR) - (g * (h0 - hR)) / (kk * gR);
-        const double sq0 = sqrt(h0);
-        const double tt = sq0 - F0 / (2.0 * sq0 * dfdh);
-        const double hm = tt * tt;
-        const double u1m = uL - (hm - hL) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hL));
-        const double u2m = uR + (hm - hR) * sqrt((0.5 * g) * (1.0 / hm + 1.0 / hR));
-        const double sqm = sqrt(g * hm);
-        s1m = u1m - sqm;
-        s2m = u2m + sqm;
-    } else {
-        const double hmn = r.lowR ? hR : hL, hmx = r.highR ? hR : hL;
-        const double sqmn = r.lowR ? sqR : sqL, sqmx = r.highR ? sqR : sqL;
-        const double F0 = delu + 2.0 * (sqmn - sqmx);
-        const double Fmax = delu + (hmx - hmn) * sqrt(((0.5 * g) * (hmx + hmn)) / (hmx * hmn));
-        const double hm = hmn - F0 / ((Fmax - F0) / (hmx - hmn));
-        const double sqm = sqrt(g * hm);
-        if (r.lhigh) {
-            s1m = (uL + 2.0 * sqL) - 3.0 * sqm;
-            s2m = (uL + 2.0 * sqL) - sqm;
-        } else {
-            s2m = (uR - 2.0 * sqR) + 3.0 * sqm;
-            s1m = (uR - 2.0 * sqR) + sqm;
-        }
-    }
+// a / b for cotangents: the reciprocal to about one ulp (rcp_nr) for a normal divisor, else IEEE
+__device__ __forceinline__ double cdiv(double a, double b) {
+    return exp_in(b, -1000, 1000) ? a * rcp_nr(b) : a / b;
 }
 
 __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, double uL, double uR, double sqL,
@@ -104,7 +67,7 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         c.sqR -= 2.0 * b2;
         const double b_sqm = 3.0 * (b2 - b1);
         const double b_hm = dsqrt(sqm, b_sqm * g);
-        const double b_t = b_hm * t * (1.0 / (8.0 * g));
+        const double b_t = b_hm * t * ((1.0 / (8.0 * g)));
         if (r.t_pos) {
             b_delu -= b_t;
             c.sqL += 2.0 * b_t;
@@ -112,16 +75,16 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         }
     } else if (r.rs == 2) {  // two shocks: one Newton step
         const double h0 = r.highR ? hR : hL;
-        const double i0 = 1.0 / h0, iL = 1.0 / hL, iR = 1.0 / hR;
+        const double i0 = cdiv(1.0, h0), iL = cdiv(1.0, hL), iR = cdiv(1.0, hR);
         const double gL = sqrt((0.5 * g) * (i0 + iL)), gR = sqrt((0.5 * g) * (i0 + iR));
         const double F0 = (delu + (h0 - hL) * gL) + (h0 - hR) * gR;
         const double kk = 4.0 * (h0 * h0);
-        const double eL = (g * (h0 - hL)) / (kk * gL), eR = (g * (h0 - hR)) / (kk * gR);
+        const double eL = cdiv((g * (h0 - hL)), (kk * gL)), eR = cdiv((g * (h0 - hR)), (kk * gR));
         const double dfdh = ((gL - eL) + gR) - eR;
         const double sq0 = sqrt(h0);
         const double slope = 2.0 * sq0 * dfdh;
-        const double tt = sq0 - F0 / slope;
-        const double hm = tt * tt, im = 1.0 / hm;
+        const double tt = sq0 - cdiv(F0, slope);
+        const double hm = tt * tt, im = cdiv(1.0, hm);
         const double cL = sqrt((0.5 * g) * (im + iL)), cR = sqrt((0.5 * g) * (im + iR));
         const double sqm = sqrt(g * hm);
         // s1m = u1m - sqm, s2m = u2m + sqm
@@ -144,8 +107,8 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         const double b_tt = 2.0 * tt * b_hm;
         // tt = sq0 - F0 / slope, slope = 2 sq0 dfdh
         double b_sq0 = b_tt;
-        const double b_F0 = -b_tt / slope;
-        const double b_slope = b_tt * F0 / (slope * slope);
+        const double b_F0 = -cdiv(b_tt, slope);
+        const double b_slope = b_tt * cdiv(F0, (slope * slope));
         b_sq0 = fma(b_slope, 2.0 * dfdh, b_sq0);
         const double b_dfdh = b_slope * 2.0 * sq0;
         b_h0 += dsqrt(sq0, b_sq0);
@@ -154,18 +117,18 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         const double b_eL = -b_dfdh, b_eR = -b_dfdh;
         double b_kk = 0.0;
         {
-            const double q = g / (kk * gL);
+            const double q = cdiv(g, (kk * gL));
             b_h0 = fma(b_eL, q, b_h0);
             b_hL = fma(-b_eL, q, b_hL);
-            b_kk = fma(-b_eL, eL / kk, b_kk);
-            b_gL = fma(-b_eL, eL / gL, b_gL);
+            b_kk = fma(-b_eL, cdiv(eL, kk), b_kk);
+            b_gL = fma(-b_eL, cdiv(eL, gL), b_gL);
         }
         {
-            const double q = g / (kk * gR);
+            const double q = cdiv(g, (kk * gR));
             b_h0 = fma(b_eR, q, b_h0);
             b_hR = fma(-b_eR, q, b_hR);
-            b_kk = fma(-b_eR, eR / kk, b_kk);
-            b_gR = fma(-b_eR, eR / gR, b_gR);
+            b_kk = fma(-b_eR, cdiv(eR, kk), b_kk);
+            b_gR = fma(-b_eR, cdiv(eR, gR), b_gR);
         }
         b_h0 = fma(b_kk, 8.0 * h0, b_h0);
         // F0 = (delu + (h0 - hL) gL) + (h0 - hR) gR
@@ -191,12 +154,12 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         const double hmn = r.lowR ? hR : hL, hmx = r.highR ? hR : hL;
         const double sqmn = r.lowR ? sqR : sqL, sqmx = r.highR ? sqR : sqL;
         const double F0 = delu + 2.0 * (sqmn - sqmx);
-        const double P = ((0.5 * g) * (hmx + hmn)) / (hmx * hmn);
+        const double P = cdiv(((0.5 * g) * (hmx + hmn)), (hmx * hmn));
         const double W = sqrt(P);
         const double Fmax = delu + (hmx - hmn) * W;
         const double den = hmx - hmn;
-        const double slope = (Fmax - F0) / den;
-        const double hm = hmn - F0 / slope;
+        const double slope = cdiv((Fmax - F0), den);
+        const double hm = hmn - cdiv(F0, slope);
         const double sqm = sqrt(g * hm);
         double b_sqm;
         if (r.lhigh) {
@@ -213,11 +176,11 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         const double b_hm = dsqrt(sqm, b_sqm * g);
         // hm = hmn - F0 / slope; slope = (Fmax - F0) / den
         double b_hmn = b_hm, b_hmx = 0.0;
-        double b_F0 = -b_hm / slope;
-        const double b_slope = b_hm * F0 / (slope * slope);
-        const double b_Fmax = b_slope / den;
-        b_F0 -= b_slope / den;
-        const double b_den = -b_slope * slope / den;
+        double b_F0 = -cdiv(b_hm, slope);
+        const double b_slope = b_hm * cdiv(F0, (slope * slope));
+        const double b_Fmax = cdiv(b_slope, den);
+        b_F0 -= cdiv(b_slope, den);
+        const double b_den = -b_slope * cdiv(slope, den);
         b_hmx += b_den;
         b_hmn -= b_den;
         // Fmax = delu + (hmx - hmn) W, W = sqrt(P), P = 0.5 g (1 / hmn + 1 / hmx)
@@ -225,8 +188,8 @@ __device__ __forceinline__ void rs_rev(const AugRec& r, double hL, double hR, do
         b_hmx = fma(b_Fmax, W, b_hmx);
         b_hmn = fma(-b_Fmax, W, b_hmn);
         const double b_P = dsqrt(W, b_Fmax * (hmx - hmn));
-        b_hmx = fma(-b_P * (0.5 * g), 1.0 / (hmx * hmx), b_hmx);
-        b_hmn = fma(-b_P * (0.5 * g), 1.0 / (hmn * hmn), b_hmn);
+        b_hmx = fma(-b_P * (0.5 * g), cdiv(1.0, (hmx * hmx)), b_hmx);
+        b_hmn = fma(-b_P * (0.5 * g), cdiv(1.0, (hmn * hmn)), b_hmn);
         // F0 = delu + 2 (sq_min - sq_max)
         b_delu += b_F0;
         if (r.lowR) c.sqR += 2.0 * b_F0;
@@ -253,8 +216,7 @@ __device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], d
                                         AugCot& c) {
     const double g = kG;
     // ---- forward values on the recorded branches
-    double s1m, s2m;
-    rs_values(r, hL, hR, uL, uR, sqL, sqR, s1m, s2m);
+    const double s1m = r.s1m, s2m = r.s2m;
     const double delh = hR - hL, delhu = huR - huL, delb = bR - bL;
     const double l0 = r.l0_sE1 ? sE1in : s2m, l2 = r.l2_sE2 ? sE2in : s1m;
     const double dsp = l2 - l0;
@@ -265,24 +227,24 @@ __device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], d
     const double s1s2bar = 0.25 * (su * su) - g * hbar;
     const double s1s2tilde = (r.tilde_x ? uL * uR : 0.0) - g * hbar;
     const double dgh = (delb * g) * hbar;
-    const double ddh0 = r.sonic ? -delb : dgh / s1s2bar;
+    const double ddh0 = r.sonic ? -delb : cdiv(dgh, s1s2bar);
     const double hsd = hstar * dsp;
     double hi = 0.0, lo = 0.0;
     if (r.dcase == 1) {
-        hi = hsd / l2;
-        lo = hsd / l0;
+        hi = cdiv(hsd, l2);
+        lo = cdiv(hsd, l0);
     } else if (r.dcase == 2) {
-        hi = hsd / l0;
+        hi = cdiv(hsd, l0);
         lo = -hL;
     } else if (r.dcase == 3) {
         hi = hR;
-        lo = hsd / l2;
+        lo = cdiv(hsd, l2);
     }
     const double x1 = r.dd_min_first ? ddh0 : hi;
     const double deldelh = r.dcase ? (r.dd_max_first ? x1 : lo) : ddh0;
     // (deldelphi and d2 = delphi - deldelphi enter beta1 only, linearly: their values are not needed)
     const double d0 = delh - deldelh, d1 = delhu;
-    const double det = l0 - l2, id = 1.0 / det;
+    const double det = l0 - l2, id = cdiv(1.0, det);
     const double beta0 = (d1 - l2 * d0) * id, beta2 = (l0 * d0 - d1) * id;
     // ---- reverse
     // fw(3,2) = (((hR uR) vR - (hL uL) vL) - fw(3,1)) - fw(3,3)
@@ -338,9 +300,9 @@ __device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], d
         b_hbar = fma(-b_ddp0, g * delb, b_hbar);
         b_delb = fma(-b_ddp0, g * hbar, b_delb);
     } else {  // -((dgh s1s2tilde) / s1s2bar)
-        b_dgh = fma(-b_ddp0, s1s2tilde / s1s2bar, b_dgh);
-        b_st = fma(-b_ddp0, dgh / s1s2bar, b_st);
-        b_sb = fma(b_ddp0, dgh * s1s2tilde / (s1s2bar * s1s2bar), b_sb);
+        b_dgh = fma(-b_ddp0, cdiv(s1s2tilde, s1s2bar), b_dgh);
+        b_st = fma(-b_ddp0, cdiv(dgh, s1s2bar), b_st);
+        b_sb = fma(b_ddp0, dgh * cdiv(s1s2tilde, (s1s2bar * s1s2bar)), b_sb);
     }
     // deldelh = max(min(ddh0, hi), lo) in the recorded case
     double b_ddh0 = 0.0;
@@ -351,17 +313,17 @@ __device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], d
         if (r.dd_min_first) b_ddh0 = b_x1;
         else b_hi = b_x1;
         if (r.dcase == 1) {  // hi = hsd / l2, lo = hsd / l0
-            b_hsd = fma(b_hi, 1.0 / l2, fma(b_lo, 1.0 / l0, b_hsd));
-            b_l2 = fma(-b_hi, hsd / (l2 * l2), b_l2);
-            b_l0 = fma(-b_lo, hsd / (l0 * l0), b_l0);
+            b_hsd = fma(b_hi, cdiv(1.0, l2), fma(b_lo, cdiv(1.0, l0), b_hsd));
+            b_l2 = fma(-b_hi, cdiv(hsd, (l2 * l2)), b_l2);
+            b_l0 = fma(-b_lo, cdiv(hsd, (l0 * l0)), b_l0);
         } else if (r.dcase == 2) {  // hi = hsd / l0, lo = -hL
-            b_hsd = fma(b_hi, 1.0 / l0, b_hsd);
-            b_l0 = fma(-b_hi, hsd / (l0 * l0), b_l0);
+            b_hsd = fma(b_hi, cdiv(1.0, l0), b_hsd);
+            b_l0 = fma(-b_hi, cdiv(hsd, (l0 * l0)), b_l0);
             c.hL -= b_lo;
         } else {  // hi = hR, lo = hsd / l2
             c.hR += b_hi;
-            b_hsd = fma(b_lo, 1.0 / l2, b_hsd);
-            b_l2 = fma(-b_lo, hsd / (l2 * l2), b_l2);
+            b_hsd = fma(b_lo, cdiv(1.0, l2), b_hsd);
+            b_l2 = fma(-b_lo, cdiv(hsd, (l2 * l2)), b_l2);
         }
     } else {
         b_ddh0 = b_ddh;
@@ -369,8 +331,8 @@ __device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], d
     if (r.sonic) {  // -delb
         b_delb -= b_ddh0;
     } else {  // dgh / s1s2bar
-        b_dgh = fma(b_ddh0, 1.0 / s1s2bar, b_dgh);
-        b_sb = fma(-b_ddh0, dgh / (s1s2bar * s1s2bar), b_sb);
+        b_dgh = fma(b_ddh0, cdiv(1.0, s1s2bar), b_dgh);
+        b_sb = fma(-b_ddh0, cdiv(dgh, (s1s2bar * s1s2bar)), b_sb);
     }
     // hsd = hstar dsp
     double b_hstar = b_hsd * dsp;
@@ -393,7 +355,7 @@ __device__ __forceinline__ void aug_rev(const AugRec& r, const double F[3][3], d
     }
     // hstar = max(q, 0), q = (((huL - huR) + l2 hR) - l0 hL) / dsp
     if (r.hst_pos) {
-        const double bq = b_hstar / dsp;
+        const double bq = cdiv(b_hstar, dsp);
         c.huL += bq;
         c.huR -= bq;
         b_l2 = fma(bq, hR, b_l2);
@@ -732,7 +694,7 @@ __device__ __forceinline__ double sgn(double x) { return lt0(x) ? -1.0 : (gt0(x)
 // Normal velocity v = n1 (p1 / d) + n2 (p2 / d): adds its cotangent bv to p1, p2 and d.
 __device__ __forceinline__ void nv_vjp(double n1, double n2, double v, double d, double bv, double& bp1,
                                        double& bp2, double& bd) {
-    const double r = 1.0 / d;
+    const double r = cdiv(1.0, d);
     bp1 = fma(bv * n1, r, bp1);
     bp2 = fma(bv * n2, r, bp2);
     bd = fma(-bv * v, r, bd);
@@ -740,7 +702,7 @@ __device__ __forceinline__ void nv_vjp(double n1, double n2, double v, double d,
 
 // d sqrt(g h) / dh times bs (0 where h = 0, as the reference gradient has it)
 __device__ __forceinline__ double sqrt_g_vjp(double h, double bs) {
-    return gt0(h) ? bs * (0.5 * kG) / sqrt(kG * h) : 0.0;
+    return gt0(h) ? cdiv(bs * (0.5 * kG), sqrt(kG * h)) : 0.0;
 }
 
 template <int SOLVER>

@@ -272,6 +272,7 @@ struct AugRec {
     int8_t dcase;      // deldelh bounds: 0 none, 1 both speeds apart, 2 sE1 >= ct, 3 sE2 <= -ct
     bool dd_min_first, dd_max_first;  // each bound kept the running value
     bool ph_mx_pl, ph_min_first, ph_mn_pl, ph_max_first;  // deldelphi bounds
+    double s1m, s2m;   // riemanntype's speeds
 };
 
 // Riemann structure with one Newton step, src/geoclaw/riemannsolvers.f:507-618.
@@ -417,6 +418,8 @@ __device__ __forceinline__ void riemann_aug_rec(double hL, double hR, double huL
     if (REC) {
         rec->l0_sE1 = lt(sE1, s2m);
         rec->l2_sE2 = lt(s1m, sE2);
+        rec->s1m = s1m;
+        rec->s2m = s2m;
     }
     sE1 = l0;
     sE2 = l2;
