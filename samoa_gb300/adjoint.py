@@ -114,13 +114,15 @@ class GaugeProblem:
         self.ctx.close()
 
     # ---- primitives
-    def _set_initial(self, h0, b):
+    def _set_initial(self, h0, b, hu0=None, hv0=None):
         h0 = torch.as_tensor(h0, dtype=torch.float64).detach().cpu().numpy()
         b = torch.as_tensor(b, dtype=torch.float64).detach().cpu().numpy()
         z = np.zeros(self.n)
+        hu0 = z if hu0 is None else torch.as_tensor(hu0, dtype=torch.float64).detach().cpu().numpy()
+        hv0 = z if hv0 is None else torch.as_tensor(hv0, dtype=torch.float64).detach().cpu().numpy()
         self.ctx.upload_mesh(self.mesh)  # resets the step count (traversal parity) to 0
         self.ctx.set_params(self.params)
-        self.ctx.upload_state(h0, z, z, b)
+        self.ctx.upload_state(h0, hu0, hv0, b)
         self.ctx.set_time(0.0, float(self.dts[0]) if self.T else 0.0)
         self.ctx.set_dt_sequence(self.dts)
 
@@ -184,11 +186,14 @@ class GaugeProblem:
         self.gauge_values = self.gv
         return J.value, gh, gb
 
-    def gradient_python(self, h0, b):
+    def gradient_python(self, h0, b, hu0=None, hv0=None, lam_end=None, full=False):
         """(J, dJ/dh0, dJ/db) from one checkpointed sweep driven from Python step
         by step: the first forward descent of the schedule records the gauges
         (for J and its residuals) and every forward step records its branches
-        for the reverse step."""
+        for the reverse step. The initial momenta (hu0, hv0) default to rest;
+        lam_end (3 x n, optional) is the cotangent of the final state, for a
+        window of a longer run. With full, the gradient in h0 is the whole
+        initial-state cotangent (3 x n)."""
         n = self.n
         L = self.ctx.L
         problem = self
@@ -196,6 +201,8 @@ class GaugeProblem:
             self.gv = torch.empty((self.T, len(self.gauges)), dtype=torch.float64, device=self.dev)
             self.done = [False] * self.T
             lam = torch.zeros((3, n), dtype=torch.float64, device=self.dev)
+            if lam_end is not None:
+                lam.copy_(torch.as_tensor(lam_end, dtype=torch.float64, device=self.dev))
             out = torch.zeros_like(lam)
             bbar = torch.zeros(n, dtype=torch.float64, device=self.dev)
             state = {"lam": lam, "out": out}
@@ -227,12 +234,12 @@ class GaugeProblem:
                 def release(self, slot):
                     problem.free.append(slot)
 
-            self._set_initial(h0, b)
+            self._set_initial(h0, b, hu0, hv0)
             self.cur = 0
             self.free = list(range(self.snapshots))
             revolve(self.T, self.snapshots, Ops())
             J = float(((self.gv - self.obs) ** 2).sum().item())
-            gh = state["lam"][0].clone()
+            gh = state["lam"].clone() if full else state["lam"][0].clone()
         self.stream.synchronize()
         self.gauge_values = self.gv
         return J, gh, bbar
@@ -267,6 +274,174 @@ def time_steps(problem, h0, b, k=50):
         e2.synchronize()
         P.free.append(slot)
     return e0.elapsed_time(e1) * 1e-3 / k, e1.elapsed_time(e2) * 1e-3 / k
+
+
+def locate_points(vertices, points):
+    """Index of the cell containing each point (unit-square coordinates; the
+    first cell in traversal order for a point on an edge): float64[n, 3, 2]
+    vertices, float64[g, 2] points -> int64[g]."""
+    v = np.asarray(vertices, np.float64)
+    a, b, c = v[:, 0], v[:, 1], v[:, 2]
+    out = np.empty(len(points), np.int64)
+    for i, (x, y) in enumerate(np.asarray(points, np.float64)):
+        def side(p, q):
+            return (q[:, 0] - p[:, 0]) * (y - p[:, 1]) - (q[:, 1] - p[:, 1]) * (x - p[:, 0])
+        s0, s1, s2 = side(a, b), side(b, c), side(c, a)
+        tol = 1e-15
+        inside = ((s0 >= -tol) & (s1 >= -tol) & (s2 >= -tol)) | ((s0 <= tol) & (s1 <= tol) & (s2 <= tol))
+        hit = np.flatnonzero(inside)
+        if len(hit) == 0:
+            raise ValueError("point (%g, %g) lies outside the mesh" % (x, y))
+        out[i] = hit[0]
+    return out
+
+
+class Transfer:
+    """The order-0 state transfer of one remesh (src/Samoa/Tools_lagrange_basis.f90:139-220):
+    a new cell copies its source cell (kept or refined) or averages two merged
+    siblings, 0.5 * (q[s] + q[s + 1]); and its adjoint."""
+
+    def __init__(self, old_depth, new_depth, src):
+        self.src = np.asarray(src, np.int64)
+        self.merged = np.asarray(new_depth, np.int64) < np.asarray(old_depth, np.int64)[self.src]
+        self.n_old = len(old_depth)
+
+    def apply(self, q):
+        q = np.asarray(q, np.float64)
+        out = q[self.src].copy()
+        m = self.merged
+        out[m] = 0.5 * (q[self.src[m]] + q[self.src[m] + 1])
+        return out
+
+    def adjoint(self, qbar):
+        qbar = np.asarray(qbar, np.float64)
+        out = np.zeros(self.n_old)
+        k = ~self.merged
+        np.add.at(out, self.src[k], qbar[k])
+        m = self.merged
+        np.add.at(out, self.src[m], 0.5 * qbar[m])
+        np.add.at(out, self.src[m] + 1, 0.5 * qbar[m])
+        return out
+
+
+class WindowedGaugeProblem:
+    """J over consecutive windows of `window` steps, each on a frozen mesh: after
+    a window the mesh is adapted from its last step's refinement flags
+    (swe_mesh_adapt: conformity closure, refine/coarsen), the state and the
+    bathymetry carried over by the order-0 transfer, and the gauge points
+    located on the new mesh. The first evaluation fixes the mesh sequence and
+    the transfers; later evaluations (objective, gradient, finite differences)
+    replay them, so J is a function of (h0, b) on the first mesh with the
+    adaptive meshes frozen per window. The gradient chains the windows'
+    checkpointed adjoints (GaugeProblem.gradient_python with the next window's
+    initial cotangent pulled back through the transfer as the final cotangent).
+
+    gauge_points: float64[G, 2] in world coordinates; obs: float64[T, G]; dts: the
+    frozen dt of each of the T steps."""
+
+    def __init__(self, mesh0, cfg, gauge_points, obs, dts, window=50, snapshots=64, device=0):
+        from .swe import mesh_from_depths
+        if mesh0.vertices is None:
+            mesh0 = mesh_from_depths(mesh0.depth, centroids=True, vertices=True)
+        self.mesh0 = mesh0
+        self.cfg = cfg
+        self.params = cfg.params()
+        pts = np.asarray(gauge_points, np.float64)
+        self.points_unit = (pts - np.asarray(cfg.offset, np.float64)) / cfg.scaling
+        self.obs = np.asarray(obs, np.float64)
+        self.dts = np.asarray(dts, np.float64)
+        self.T = len(self.dts)
+        self.window = int(window)
+        self.snapshots = int(snapshots)
+        self.device = device
+        self.plan = None
+        self.stats = {"windows": 0, "cells": []}
+
+    def _windows(self):
+        return [(k, min(k + self.window, self.T)) for k in range(0, self.T, self.window)]
+
+    def _forward(self, h0, b0, record_plan):
+        """Run all windows from (h0, b0) at rest; returns J, the initial states of
+        the windows and (first run) the meshes, gauges and transfers."""
+        from .swe import adapt
+        ctx = SweContext(self.device)
+        try:
+            ctx.set_params(self.params)
+            h, hu, hv = (np.asarray(h0, np.float64).copy(), np.zeros(self.mesh0.n_cells),
+                         np.zeros(self.mesh0.n_cells))
+            b = np.asarray(b0, np.float64).copy()
+            starts, J = [], 0.0
+            meshes, gauges, transfers = ([], [], []) if record_plan else (None, None, None)
+            mesh = self.mesh0
+            for w, (t0, t1) in enumerate(self._windows()):
+                if not record_plan:
+                    mesh = self.plan["meshes"][w]
+                gw = locate_points(mesh.vertices, self.points_unit) if record_plan else self.plan["gauges"][w]
+                if record_plan:
+                    meshes.append(mesh)
+                    gauges.append(gw)
+                starts.append((h.copy(), hu.copy(), hv.copy(), b.copy()))
+                ctx.upload_mesh(mesh)
+                ctx.upload_state(h, hu, hv, b)
+                ctx.set_time(0.0, float(self.dts[t0]))
+                ctx.set_dt_sequence(self.dts[t0:t1])
+                dev = torch.device("cuda", self.device)
+                gi = torch.as_tensor(gw, dtype=torch.int64, device=dev)
+                gv = torch.empty((t1 - t0, len(gw)), dtype=torch.float64, device=dev)
+                _lib.check(ctx.L.swe_traverse_gauges(ctx.ptr, t1 - t0, len(gw), _vp(gi), _vp(gv)))
+                ctx.synchronize()
+                J += float(((gv.cpu().numpy() - self.obs[t0:t1]) ** 2).sum())
+                h, hu, hv, _ = ctx.download_state()
+                if t1 < self.T:
+                    if record_plan:
+                        flags, _ = ctx.refinements()
+                        new, _, src = adapt(mesh, flags, with_source=True)
+                        tr = Transfer(mesh.depth, new.depth, src)
+                        transfers.append(tr)
+                        mesh = new
+                    else:
+                        tr = self.plan["transfers"][w]
+                    h, hu, hv, b = tr.apply(h), tr.apply(hu), tr.apply(hv), tr.apply(b)
+            if record_plan:
+                self.plan = {"meshes": meshes, "gauges": gauges, "transfers": transfers}
+                self.stats["cells"] = [m.n_cells for m in meshes]
+            return J, starts
+        finally:
+            ctx.close()
+
+    def objective(self, h0, b0):
+        J, _ = self._forward(h0, b0, self.plan is None)
+        return J
+
+    def gradient(self, h0, b0):
+        """(J, dJ/dh0, dJ/db0) on the first mesh."""
+        J, starts = self._forward(h0, b0, self.plan is None)
+        wins = self._windows()
+        lam_end, bbar_next = None, None
+        Jsum = 0.0
+        for w in range(len(wins) - 1, -1, -1):
+            t0, t1 = wins[w]
+            mesh = self.plan["meshes"][w]
+            h, hu, hv, b = starts[w]
+            P = GaugeProblem(mesh, self.params, self.plan["gauges"][w], self.obs[t0:t1], self.dts[t0:t1],
+                             snapshots=min(self.snapshots, t1 - t0), device=self.device)
+            try:
+                Jw, lam0, bbar = P.gradient_python(h, b, hu, hv, lam_end=lam_end, full=True)
+                lam0 = lam0.cpu().numpy()
+                bbar = bbar.cpu().numpy()
+            finally:
+                P.close()
+            Jsum += Jw
+            if bbar_next is not None:
+                bbar = bbar + bbar_next
+            if w > 0:
+                tr = self.plan["transfers"][w - 1]
+                lam_end = np.stack([tr.adjoint(lam0[q]) for q in range(3)])
+                bbar_next = tr.adjoint(bbar)
+            else:
+                gh, gb = lam0[0], bbar
+        self.stats["windows"] = len(wins)
+        return Jsum, gh, gb
 
 
 class GaugeMisfit(torch.autograd.Function):
