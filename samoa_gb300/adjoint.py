@@ -113,6 +113,26 @@ class GaugeProblem:
         self.stream.synchronize()
         self.ctx.close()
 
+    def retarget(self, mesh, gauges, obs, dts):
+        """The same problem object on another mesh (and gauges, observations, dt
+        sequence): the context's buffers and the snapshot and branch buffers are
+        reused where they fit (a windowed run moves through many meshes)."""
+        self.stream.synchronize()
+        self.mesh = mesh
+        self.n = mesh.n_cells
+        self.stride = (self.n + 1) & ~1
+        self.dts = np.ascontiguousarray(dts, np.float64)
+        self.T = len(self.dts)
+        with torch.cuda.stream(self.stream):
+            self.gauges = torch.as_tensor(np.asarray(gauges, np.int64), device=self.dev)
+            self.obs = torch.as_tensor(np.asarray(obs, np.float64), device=self.dev)
+            if self.slots.shape[2] < self.n:
+                self.slots = torch.empty((self.snapshots, 3, self.n), dtype=torch.float64, device=self.dev)
+            if self.branches.shape[0] < self.T or self.branches.shape[1] < self.stride:
+                self.branches = torch.empty((max(self.T, self.branches.shape[0]), self.stride), dtype=torch.uint8,
+                                            device=self.dev)
+        # the mesh goes to the device with the next initial state (_set_initial)
+
     # ---- primitives
     def _set_initial(self, h0, b, hu0=None, hv0=None):
         h0 = torch.as_tensor(h0, dtype=torch.float64).detach().cpu().numpy()
@@ -128,14 +148,14 @@ class GaugeProblem:
 
     def _store(self, step):
         slot = self.free.pop()
-        s = self.slots[slot]
+        s = self.slots[slot][:, :self.n]
         got = C.c_int64()
         _lib.check(self.ctx.L.swe_snapshot_store(self.ctx.ptr, _vp(s[0]), _vp(s[1]), _vp(s[2]), C.byref(got)))
         assert got.value == step, (got.value, step)
         return slot
 
     def _restore(self, slot, step):
-        s = self.slots[slot]
+        s = self.slots[slot][:, :self.n]
         _lib.check(self.ctx.L.swe_snapshot_restore(self.ctx.ptr, _vp(s[0]), _vp(s[1]), _vp(s[2]), step))
         self.cur = step
 
@@ -419,27 +439,29 @@ class WindowedGaugeProblem:
         wins = self._windows()
         lam_end, bbar_next = None, None
         Jsum = 0.0
-        for w in range(len(wins) - 1, -1, -1):
-            t0, t1 = wins[w]
-            mesh = self.plan["meshes"][w]
-            h, hu, hv, b = starts[w]
-            P = GaugeProblem(mesh, self.params, self.plan["gauges"][w], self.obs[t0:t1], self.dts[t0:t1],
-                             snapshots=min(self.snapshots, t1 - t0), device=self.device)
-            try:
+        big = max(range(len(wins)), key=lambda w: self.plan["meshes"][w].n_cells)
+        P = GaugeProblem(self.plan["meshes"][big], self.params, self.plan["gauges"][big],
+                         self.obs[wins[big][0]:wins[big][1]], self.dts[wins[big][0]:wins[big][1]],
+                         snapshots=min(self.snapshots, self.window), device=self.device)
+        try:
+            for w in range(len(wins) - 1, -1, -1):
+                t0, t1 = wins[w]
+                h, hu, hv, b = starts[w]
+                P.retarget(self.plan["meshes"][w], self.plan["gauges"][w], self.obs[t0:t1], self.dts[t0:t1])
                 Jw, lam0, bbar = P.gradient_python(h, b, hu, hv, lam_end=lam_end, full=True)
                 lam0 = lam0.cpu().numpy()
                 bbar = bbar.cpu().numpy()
-            finally:
-                P.close()
-            Jsum += Jw
-            if bbar_next is not None:
-                bbar = bbar + bbar_next
-            if w > 0:
-                tr = self.plan["transfers"][w - 1]
-                lam_end = np.stack([tr.adjoint(lam0[q]) for q in range(3)])
-                bbar_next = tr.adjoint(bbar)
-            else:
-                gh, gb = lam0[0], bbar
+                Jsum += Jw
+                if bbar_next is not None:
+                    bbar = bbar + bbar_next
+                if w > 0:
+                    tr = self.plan["transfers"][w - 1]
+                    lam_end = np.stack([tr.adjoint(lam0[q]) for q in range(3)])
+                    bbar_next = tr.adjoint(bbar)
+                else:
+                    gh, gb = lam0[0], bbar
+        finally:
+            P.close()
         self.stats["windows"] = len(wins)
         return Jsum, gh, gb
 
