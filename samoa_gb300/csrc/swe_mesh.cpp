@@ -264,68 +264,94 @@ int export_mesh(const BuiltMesh& m, int8_t* depth_out, int8_t* plotter_out, int6
 // segment, then inner edges in stream (first-touch) order.
 // Direction of the outward normal of local edge k (0..2) of a cell with plotter
 // type p: 1 = along x, 2 = along y, 0 = diagonal.
+// Direction of the outward normal of local edge k of a cell of plotter type p:
+// 0 diagonal, 1 along x, 2 along y (a table built once, thread-safe).
 static int normal_axis(int p, int k) {
-    static double normal[17][3][2];
-    static bool ready = false;
-    if (!ready) {
-        double leg[kMaxDepth + 2], vol[kMaxDepth + 1];
-        geometry_tables(leg, vol, normal);
-        ready = true;
-    }
-    const double* n = normal[p + 8][k];
-    if (n[1] == 0.0 && n[0] != 0.0) return 1;
-    if (n[0] == 0.0 && n[1] != 0.0) return 2;
-    return 0;
+    struct AxisTable {
+        int8_t axis[17][3];
+        AxisTable() {
+            double normal[17][3][2], leg[kMaxDepth + 2], vol[kMaxDepth + 1];
+            geometry_tables(leg, vol, normal);
+            for (int q = 0; q < 17; ++q)
+                for (int e = 0; e < 3; ++e) {
+                    const double* nv = normal[q][e];
+                    axis[q][e] = (nv[1] == 0.0 && nv[0] != 0.0) ? 1 : (nv[0] == 0.0 && nv[1] != 0.0) ? 2 : 0;
+                }
+        }
+    };
+    static const AxisTable table;
+    return table.axis[p + 8][k];
 }
 
+// The segment lists: per segment the edges to compute, diagonal ones first, then
+// the axis-aligned ones (so a warp's tasks mostly take the same branch of the
+// flux's rotation), then the halo tasks, each class in input order (boundary
+// edges, then inner edges). Placed by counting, no sort.
 int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std::vector<int64_t>& seg_ptr,
                 std::vector<SegInfo>& seg_info, std::vector<Task>& tasks, std::vector<Task>& xtasks) {
     const int64_t n = m.n_cells;
     const int64_t nseg = (n + T - 1) / T;
     if (seg_ptr.empty()) seg_ptr.push_back(0);
     const size_t s0 = seg_info.size();
-    std::vector<int64_t> count((size_t)nseg + 1, 0);
-    for (int64_t e = 0; e < m.n_edges; ++e) {
-        int64_t sa = m.ea[(size_t)e] / T, sb = m.eb[(size_t)e] / T;
-        count[(size_t)sa + 1]++;
-        if (sb != sa) count[(size_t)sb + 1]++;
+    // task kinds: boundary edges and the inner edges inside one segment are class 0
+    // (diagonal) or 1 (axis-aligned); an inner edge between two segments is class 2
+    // (a halo task) in both
+    std::vector<int8_t> bnd_axis((size_t)m.n_bnd), edge_axis((size_t)m.n_edges);
+    std::vector<int64_t> cnt((size_t)(3 * nseg), 0);
+    for (int64_t j = 0; j < m.n_bnd; ++j) {
+        const int64_t c = m.bc[(size_t)j];
+        bnd_axis[(size_t)j] = (int8_t)normal_axis(m.plotter[(size_t)c], m.bl[(size_t)j] - 1);
+        cnt[(size_t)(3 * (c / T) + (bnd_axis[(size_t)j] ? 1 : 0))]++;
     }
-    for (int64_t j = 0; j < m.n_bnd; ++j) count[(size_t)(m.bc[(size_t)j] / T) + 1]++;
-    for (int64_t s = 0; s < nseg; ++s) count[(size_t)s + 1] += count[(size_t)s];
+    for (int64_t e = 0; e < m.n_edges; ++e) {
+        const int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
+        edge_axis[(size_t)e] = (int8_t)normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1);
+        const int64_t sa = a / T, sb = b / T;
+        if (sa == sb) {
+            cnt[(size_t)(3 * sa + (edge_axis[(size_t)e] ? 1 : 0))]++;
+        } else {
+            cnt[(size_t)(3 * sa + 2)]++;
+            cnt[(size_t)(3 * sb + 2)]++;
+        }
+    }
     const int64_t base = seg_ptr.back();
-    for (int64_t s = 0; s < nseg; ++s) {
-        seg_ptr.push_back(base + count[(size_t)s + 1]);
+    std::vector<int64_t> fill((size_t)(3 * nseg));
+    int64_t pos = base;
+    for (int64_t sg = 0; sg < nseg; ++sg) {
+        for (int k = 0; k < 3; ++k) {
+            fill[(size_t)(3 * sg + k)] = pos;
+            pos += cnt[(size_t)(3 * sg + k)];
+        }
+        seg_ptr.push_back(pos);
         SegInfo si;
-        si.c0 = (int32_t)(offset + s * T);
-        si.cn = (int32_t)std::min<int64_t>(T, n - s * T);
+        si.c0 = (int32_t)(offset + sg * T);
+        si.cn = (int32_t)std::min<int64_t>(T, n - sg * T);
         si.inst = inst;
-        si.halo = 0;
+        si.halo = (int32_t)cnt[(size_t)(3 * sg + 2)];
         seg_info.push_back(si);
     }
-    tasks.resize((size_t)(base + count[(size_t)nseg]));
-    std::vector<int64_t> fill(count.begin(), count.end() - 1);
-    for (auto& f : fill) f += base;
+    (void)s0;
+    tasks.resize((size_t)pos);
     for (int64_t j = 0; j < m.n_bnd; ++j) {
-        int64_t c = m.bc[(size_t)j];
+        const int64_t c = m.bc[(size_t)j];
         Task t;
         t.a = (int32_t)(offset + c);
         t.b = -1;
-        t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true,
-                           normal_axis(m.plotter[(size_t)c], m.bl[(size_t)j] - 1));
+        t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true, bnd_axis[(size_t)j]);
         t.pad = 0;
-        tasks[(size_t)fill[(size_t)(c / T)]++] = t;
+        tasks[(size_t)fill[(size_t)(3 * (c / T) + (bnd_axis[(size_t)j] ? 1 : 0))]++] = t;
     }
     for (int64_t e = 0; e < m.n_edges; ++e) {
-        int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
+        const int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
         Task t;
         t.a = (int32_t)(offset + a);
         t.b = (int32_t)(offset + b);
         t.meta = pack_meta(m.la[(size_t)e] - 1, m.lb[(size_t)e] - 1, m.plotter[(size_t)a], m.plotter[(size_t)b], false,
-                           normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1));
+                           edge_axis[(size_t)e]);
         t.pad = 0;
-        int64_t sa = a / T, sb = b / T;
+        const int64_t sa = a / T, sb = b / T;
         if (sb == sa) {
-            tasks[(size_t)fill[(size_t)sa]++] = t;
+            tasks[(size_t)fill[(size_t)(3 * sa + (edge_axis[(size_t)e] ? 1 : 0))]++] = t;
             continue;
         }
         // an edge between two segments: computed once by the cross-edge pass,
@@ -336,18 +362,8 @@ int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std:
         h.pad = (uint32_t)xtasks.size();
         t.pad = (uint32_t)inst;
         xtasks.push_back(t);
-        tasks[(size_t)fill[(size_t)sa]++] = h;
-        tasks[(size_t)fill[(size_t)sb]++] = h;
-        seg_info[s0 + (size_t)sa].halo++;
-        seg_info[s0 + (size_t)sb].halo++;
-    }
-    // within a segment: the edges to compute, diagonal ones first, then the
-    // axis-aligned ones (so a warp's tasks mostly take the same branch of the
-    // flux's rotation), then the halo tasks
-    for (int64_t s = 0; s < nseg; ++s) {
-        auto first = tasks.begin() + (base + count[(size_t)s]), last = tasks.begin() + (base + count[(size_t)s + 1]);
-        auto mid = std::stable_partition(first, last, [](const Task& t) { return !(t.meta & kHaloBit); });
-        std::stable_partition(first, mid, [](const Task& t) { return ((t.meta >> 15) & 3u) == 0; });
+        tasks[(size_t)fill[(size_t)(3 * sa + 2)]++] = h;
+        tasks[(size_t)fill[(size_t)(3 * sb + 2)]++] = h;
     }
     return SWE_OK;
 }
