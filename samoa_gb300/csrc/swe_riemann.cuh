@@ -303,7 +303,8 @@ __device__ __forceinline__ void riemann_structure_rec(double hL, double hR, doub
         return;
     }
     double F_min = delu + scale_pow2(sq_min - sq_max, 1, 2.0);
-    double F_max = delu + (h_max - h_min) * sqrt(((0.5 * g) * (h_max + h_min)) / (h_max * h_min));
+    double F_max = 0.0;  // needed only when F_min <= 0
+    if (!gt0(F_min)) F_max = delu + (h_max - h_min) * sqrt(((0.5 * g) * (h_max + h_min)) / (h_max * h_min));
     if (gt0(F_min)) {  // two rarefactions
         const double t0 = -delu + scale_pow2(sqL + sqR, 1, 2.0);
         double t = imax(0.0, t0);
