@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--adjoint-log2-cells", type=int, default=18)
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--adjoint-fd", type=int, default=16)
+    ap.add_argument("--adjoint-fd-frozen", type=int, default=8,
+                    help="directions of the branch-frozen finite-difference check of the adjoint")
     ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
@@ -368,6 +370,24 @@ def adjoint_compare(a, device):
                 errs[key].append(abs((Jp - Jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
                 if key == "h0":
                     nerr.append(abs((Jp - Jm) / (2 * eps) - ad) / max(np.linalg.norm(gh) * np.linalg.norm(d), 1e-300))
+        # the same check on the branch-frozen J (every decision of the unperturbed run
+        # replayed): 4-point central differences, no kink crossed
+        P.objective_frozen(case["h0"], case["b"], record=True)
+        ferrs = []
+        for k in range(a.adjoint_fd_frozen):
+            d = rng.normal(size=gh.shape)
+            eps = 1e-4 * float(np.abs(case["h0"]).max())  # smooth J: the round-off of J sets the step
+            Jf = lambda s_: P.objective_frozen(case["h0"] + s_ * eps * d, case["b"], record=False)
+            fd = (8.0 * (Jf(1) - Jf(-1)) - (Jf(2) - Jf(-2))) / (12.0 * eps)
+            ad = float(gh @ d)
+            ferrs.append(abs(fd - ad) / max(abs(ad), 1e-300))
+        fb = None
+        if a.adjoint_fd_frozen:
+            d = gb / np.linalg.norm(gb)
+            eps = 1e-4 * float(np.abs(case["b"]).max())
+            Jf = lambda s_: P.objective_frozen(case["h0"], case["b"] + s_ * eps * d, record=False)
+            fd = (8.0 * (Jf(1) - Jf(-1)) - (Jf(2) - Jf(-2))) / (12.0 * eps)
+            fb = abs(fd - float(gb @ d)) / abs(float(gb @ d))
         t_step, t_adj = adjoint.time_steps(P, case["h0"], case["b"], 50)
     finally:
         P.close()
@@ -381,6 +401,8 @@ def adjoint_compare(a, device):
             "fd_directions_h0_within_1e-6": int(sum(e <= 1e-6 for e in errs["h0"])),
             "fd_max_err_over_grad_norm_h0": max(nerr, default=None),
             "fd_directions_b": len(errs["b"]), "fd_max_rel_err_b_unfrozen": max(errs["b"], default=None),
+            "fd_frozen_directions_h0": len(ferrs), "fd_frozen_max_rel_err_h0": max(ferrs, default=None),
+            "fd_frozen_rel_err_b_along_gradient": fb,
             "forward_step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj, "adjoint_step_over_forward_step": t_adj / t_step,
             "windowed": windowed,
             "note": "gradient_s = one checkpointed sweep (its first descent is the forward run; recomputation "
@@ -389,7 +411,9 @@ def adjoint_compare(a, device):
                     "smooth: in the nearly still basin the f-wave's middle wave speed 0.5 (s1 + s2) sits near 0, and "
                     "its sign sends the shear wave to the left or the right cell, so perturbations flip branches and "
                     "J jumps slightly; the per-direction error is branch-limited (measured: not monotone in eps, "
-                    "no better with a 4-point stencil), the error against |g| |d| stays small; perturbing b "
+                    "no better with a 4-point stencil), the error against |g| |d| stays small; fd_frozen_*: the same "
+                    "check on the branch-frozen J (swe_traverse_frozen replays every decision of the unperturbed "
+                    "run), 4-point stencil, where it is not branch-limited; perturbing b "
                     "reorders neighbouring depths at rest and so crosses the Einfeldt min/max kinks over 2,000 "
                     "steps, so plain FD in b is kink-limited (the branch-frozen FD check of b is in the tests)"}
 

@@ -272,6 +272,19 @@ int swe_snapshot_restore(swe_ctx* ctx, const double* h, const double* hu, const 
  * device (the point output of src/SWE/SWE_point_output.f90:226-266 at order 0). */
 int swe_sample_gauges(swe_ctx* ctx, int64_t n_gauges, const int64_t* cells, double* out);
 
+/* Branch-frozen forward run for checking the adjoint (f-wave, single
+ * instance): mode 1 runs n_steps steps recording every edge's decisions
+ * (edges[s * edge_stride + k], edge_stride >= the task count plus the
+ * cross-segment edge count of swe_get_task_counts) and every cell's wet/dry
+ * fixes (branch[s * branch_stride + cell]); mode 2 runs them again taking
+ * every decision from those records instead of the comparisons, so the run is
+ * a smooth function of its inputs near the recorded one (finite differences of
+ * it approximate the discrete adjoint's gradient without crossing a kink).
+ * With n_gauges > 0 the gauge cells' surface after every step goes to
+ * out[s * n_gauges + g] (device memory). No reference counterpart. */
+int swe_traverse_frozen(swe_ctx* ctx, int64_t n_steps, int32_t mode, uint8_t* branch, int64_t branch_stride,
+                        uint16_t* edges, int64_t edge_stride, int64_t n_gauges, const int64_t* cells, double* out);
+
 /* Run n_steps steps like swe_traverse and record each step's wet/dry branches
  * (per cell: bit 0 wetting fix, bit 1 drying clamp) at branch + i * stride
  * for the i-th step (device buffer, stride >= n_cells). */

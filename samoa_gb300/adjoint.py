@@ -185,6 +185,30 @@ class GaugeProblem:
             self.gauge_values = gv
         return J
 
+    def objective_frozen(self, h0, b, record):
+        """J of a branch-frozen forward run (swe_traverse_frozen, the f-wave):
+        record=True runs from (h0, b) recording every edge's and cell's branch
+        decisions; record=False runs again taking every decision from the last
+        recording, so J is smooth near the recorded run and its finite
+        differences check the discrete adjoint without crossing a kink."""
+        self._set_initial(h0, b)
+        L = self.ctx.L
+        counts = self.ctx.task_counts()
+        es = counts["tasks"] + counts["cross_edges"]
+        with torch.cuda.stream(self.stream):
+            if record or getattr(self, "frozen", None) is None:
+                self.frozen = (torch.empty((self.T, self.stride), dtype=torch.uint8, device=self.dev),
+                               torch.empty((self.T, es), dtype=torch.int16, device=self.dev))
+            br, ed = self.frozen
+            if ed.shape[1] != es:
+                raise ValueError("the recording belongs to another mesh")
+            gv = torch.empty((self.T, len(self.gauges)), dtype=torch.float64, device=self.dev)
+            _lib.check(L.swe_traverse_frozen(self.ctx.ptr, self.T, 1 if record else 2, _vp(br), self.stride, _vp(ed),
+                                             es, len(self.gauges), _vp(self.gauges), _vp(gv)))
+            J = float(((gv - self.obs) ** 2).sum().item())
+        self.stats["forward_steps"] += self.T
+        return J
+
     def gradient(self, h0, b):
         """(J, dJ/dh0, dJ/db) from one checkpointed sweep run inside the library
         (swe_gauge_gradient: the same schedule as gradient_python, no host round

@@ -58,6 +58,8 @@ struct StepArgs {
     const int4* xtasks;        // cross-segment edges (Task layout, pad = instance)
     double* xflux;             // [n_xtasks][cell a, cell b][h, hu, hv, max wave speed] of the current step
     long long n_xtasks;
+    uint16_t* erec;            // branch-frozen runs: this step's edge decisions, per task ...
+    uint16_t* xrec;            // ... and per cross-segment edge
     const InstParams* ip;
     InstScalars* is;
     GlobalScalars* gs;
@@ -188,7 +190,7 @@ __device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, doub
 // The edges between two segments, one thread each, before the step kernel:
 // the same flux as the step kernel's edge tasks (orientation by the step's
 // parity, pre-update states), both sides' updates stored by cell (a, then b).
-template <int SOLVER>
+template <int SOLVER, int FZ = 0>
 __global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= A.n_xtasks) return;
@@ -221,7 +223,8 @@ __global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
     depth_terms(QL, drytol, dL, sqL, yL);
     depth_terms(QR, drytol, dR, sqR, yR);
     Update fL, fR;
-    edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, (int)((meta >> 15) & 3u));
+    edge_flux<SOLVER, FZ>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, (int)((meta >> 15) & 3u),
+                          FZ ? &A.xrec[j] : nullptr);
     const Update& ua = odd ? fR : fL;
     const Update& ub = odd ? fL : fR;
     double2* out = reinterpret_cast<double2*>(A.xflux + 8 * j);
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
     out[3] = make_double2(ub.p2, ub.s);
 }
 
-template <int SOLVER>
+template <int SOLVER, int FZ = 0>
 __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int T = A.seg_cells;
@@ -455,7 +458,8 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
                 depth_terms(QR, P.drytol, dR, sqR, yR);
             }
             Update fL, fR;
-            edge_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, fL, fR, (int)((meta >> 15) & 3u));
+            edge_flux<SOLVER, FZ>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, fL, fR,
+                                  (int)((meta >> 15) & 3u), FZ ? &A.erec[t] : nullptr);
             if (lin) {
                 upd[(0 * 3 + iL) * T + sl] = fL.h;
                 upd[(1 * 3 + iL) * T + sl] = fL.p1;
@@ -532,7 +536,9 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             const double b = sh_b[i];
             uint8_t br = 0;
             const double bdry = b + P.drytol;
-            if (lt(h, bdry) && gt0(dh)) {  // flooded land starts at the dry tolerance, at rest
+            const uint8_t rb = FZ == 2 ? A.branch[c] : 0;  // a branch-frozen run takes the recorded fixes
+            // flooded land starts at the dry tolerance, at rest
+            if (FZ == 2 ? (rb & 1u) != 0 : (lt(h, bdry) && gt0(dh))) {
                 h = bdry;
                 p1 = 0.0;
                 p2 = 0.0;
@@ -547,13 +553,13 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
                 p1 = p1 + dp1;
                 p2 = p2 + dp2;
             }
-            if (lt(h, bdry)) {  // dried out: surface to min(b, 0), at rest
+            if (FZ == 2 ? (rb & 2u) != 0 : lt(h, bdry)) {  // dried out: surface to min(b, 0), at rest
                 h = lt0(b) ? b : 0.0;
                 p1 = 0.0;
                 p2 = 0.0;
                 br |= 2;
             }
-            if (A.branch) A.branch[c] = br;
+            if (FZ != 2 && A.branch) A.branch[c] = br;
             hout[c] = h;
             huout[c] = p1;
             hvout[c] = p2;

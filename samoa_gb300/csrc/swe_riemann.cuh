@@ -551,51 +551,79 @@ static __device__ __noinline__ void riemann_aug(double hL, double hR, double huL
 // caller; they are used only where the reference evaluates sqrt(g * h) on an
 // unmodified wet depth (the same operands, so the same bits).
 // yL0 / yR0 are RN(1 / depth) of the two cells (read only for wet sides).
-template <int SOLVER>
+// Branch-frozen evaluation (FZ, the f-wave only): FZ = 1 records the decisions
+// of the edge into *fz, FZ = 2 takes them from *fz instead of the comparisons
+// (a forward run whose every branch is that of a recorded run, for checking the
+// discrete adjoint by finite differences). Bits: 0 both sides dry, 1 right wet,
+// 2 left wet, 3 right wall, 4 right bottom lowered, 5 left wall, 6 left bottom
+// lowered, 7 sE1 = sL, 8 sE2 = sR, 9 + 2w / 10 + 2w wave w's speed < 0 / > 0.
+template <int FZ>
+__device__ __forceinline__ bool fzb(uint16_t* fz, int bit, bool v) {
+    if (FZ == 2) return (*fz >> bit) & 1u;
+    if (FZ == 1 && v) *fz |= (uint16_t)(1u << bit);
+    return v;
+}
+
+template <int SOLVER, int FZ = 0>
 __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL, double huR, double hvL,
                                                double hvR, double bL, double bR, double sqL0, double sqR0,
                                                double yL0, double yR0, double drytol, double netL[3],
-                                               double netR[3], double& maxspeed) {
+                                               double netR[3], double& maxspeed, uint16_t* fz = nullptr) {
     const double g = kG;
     netL[0] = netL[1] = netL[2] = 0.0;
     netR[0] = netR[1] = netR[2] = 0.0;
     maxspeed = 0.0;
-    const bool wetR0 = lt(drytol, hR), wetL0 = lt(drytol, hL);  // h > drytol
-    if (!wetL0 && !wetR0 && !is_nan(hL) && !is_nan(hR) && !is_nan(drytol)) return;  // both h <= drytol
+    if (FZ == 1) *fz = 0;
+    const bool wetR0 = fzb<FZ>(fz, 1, lt(drytol, hR)), wetL0 = fzb<FZ>(fz, 2, lt(drytol, hL));  // h > drytol
+    if (fzb<FZ>(fz, 0, !wetL0 && !wetR0 && !is_nan(hL) && !is_nan(hR) && !is_nan(drytol))) return;  // both dry
+    if (FZ == 2) {  // a recorded wet side is wet here, whatever its current depth
+        if (wetL0) sqL0 = sqrt(g * hL);
+        if (wetR0) sqR0 = sqrt(g * hR);
+    }
     double uL, uR, vL, vR;
     if (wetR0) {
-        const Recip r{hR, yR0, recip_fast(hR)};
-        uR = div_rn(huR, r);
-        vR = div_rn(hvR, r);
+        if (FZ == 2) {
+            uR = huR / hR;
+            vR = hvR / hR;
+        } else {
+            const Recip r{hR, yR0, recip_fast(hR)};
+            uR = div_rn(huR, r);
+            vR = div_rn(hvR, r);
+        }
     } else {
         hR = 0.0; huR = 0.0; hvR = 0.0; uR = 0.0; vR = 0.0;
     }
     if (wetL0) {
-        const Recip r{hL, yL0, recip_fast(hL)};
-        uL = div_rn(huL, r);
-        vL = div_rn(hvL, r);
+        if (FZ == 2) {
+            uL = huL / hL;
+            vL = hvL / hL;
+        } else {
+            const Recip r{hL, yL0, recip_fast(hL)};
+            uL = div_rn(huL, r);
+            vL = div_rn(hvL, r);
+        }
     } else {
         hL = 0.0; huL = 0.0; hvL = 0.0; uL = 0.0; vL = 0.0;
     }
     bool wall_l = false, wall_r = false;  // wall(1) = 0 resp. wall(3) = 0 (wall(2) = 0 with either)
     if (!wetR0) {  // hR is now 0.0, and 0.0 <= drytol
-        double hstar, s1m, s2m;
-        riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);  // a rare edge: sqrt here
+        double hstar = 0.0, s1m, s2m;
+        if (FZ != 2) riemann_structure(hL, hL, uL, -uL, drytol, hstar, s1m, s2m);  // a rare edge: sqrt here
         double hstartest = dmx(hL, hstar);
-        if (hstartest + bL < bR) {
+        if (fzb<FZ>(fz, 3, hstartest + bL < bR)) {
             wall_r = true;
             hR = hL; huR = -huL; bR = bL; uR = -uL; vR = vL;
-        } else if (hL + bL < bR) {
+        } else if (fzb<FZ>(fz, 4, hL + bL < bR)) {
             bR = hL + bL;
         }
     } else if (!wetL0) {
-        double hstar, s1m, s2m;
-        riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);  // a rare edge: sqrt here
+        double hstar = 0.0, s1m, s2m;
+        if (FZ != 2) riemann_structure(hR, hR, -uR, uR, drytol, hstar, s1m, s2m);  // a rare edge: sqrt here
         double hstartest = dmx(hR, hstar);
-        if (hstartest + bR < bL) {
+        if (fzb<FZ>(fz, 5, hstartest + bR < bL)) {
             wall_l = true;
             hL = hR; huL = -huR; bL = bR; uL = -uR; vL = vR;
-        } else if (hR + bR < bL) {
+        } else if (fzb<FZ>(fz, 6, hR + bR < bL)) {
             bL = hR + bR;
         }
     }
@@ -614,8 +642,9 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     double sR = uR + sqR;
     double uhat = div_rn(imul(sqL, uL) + imul(sqR, uR), recip_rn(sqR + sqL));
     double chat = sqrt(ghalf_h);
-    double sE1 = imin(sL, uhat - chat);
-    double sE2 = imax(sR, uhat + chat);
+    const double r1 = uhat - chat, r2 = uhat + chat;
+    double sE1 = fzb<FZ>(fz, 7, lt(sL, r1)) ? sL : r1;  // imin(sL, r1)
+    double sE2 = fzb<FZ>(fz, 8, lt(r2, sR)) ? sR : r2;  // imax(sR, r2)
 
     double sw[3], fw[3][3];
     if (SOLVER == AUG_RIEMANN) {
@@ -662,7 +691,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     };
 #pragma unroll
     for (int w = 0; w < 3; ++w) {
-        const bool neg = lt0(sw[w]), pos = gt0(sw[w]);
+        const bool neg = fzb<FZ>(fz, 9 + 2 * w, lt0(sw[w])), pos = fzb<FZ>(fz, 10 + 2 * w, gt0(sw[w]));
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
             if (SOLVER != AUG_RIEMANN && w == 1 && e < 2) continue;
@@ -696,13 +725,17 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
 // (|n1| = |n2| = c) the four products of each rotation are +-RN(c p1) and
 // +-RN(c p2), since RN(-x) = -RN(x): two products per side, the signs set on
 // the bit patterns. Otherwise the general form runs.
-template <int SOLVER>
+template <int SOLVER, int FZ = 0>
 __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& QL, const State& QR, double dL,
                                              double dR, double sqL, double sqR, double yL, double yR,
-                                             double drytol, Update& fL, Update& fR, int axis = 0) {
+                                             double drytol, Update& fL, Update& fR, int axis = 0,
+                                             uint16_t* fz = nullptr) {
     // both sides dry: the solver returns zero net updates and speed, and their
     // rotation back is +0 in every component, so neither rotation is needed
-    if (!lt(drytol, dL) && !lt(drytol, dR) && !is_nan(dL) && !is_nan(dR) && !is_nan(drytol)) {
+    const bool dry2 = FZ == 2 ? ((*fz & 1u) != 0)
+                              : (!lt(drytol, dL) && !lt(drytol, dR) && !is_nan(dL) && !is_nan(dR) && !is_nan(drytol));
+    if (dry2) {
+        if (FZ == 1) *fz = 1;
         fL = Update{0.0, 0.0, 0.0, 0.0};
         fR = Update{0.0, 0.0, 0.0, 0.0};
         return;
@@ -738,7 +771,8 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         pR2 = z0(imul_rot(-n2, QR.p1)) + imul_rot(n1, QR.p2);
     }
     double netL[3], netR[3], ms;
-    geoclaw_solver<SOLVER>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, yL, yR, drytol, netL, netR, ms);
+    geoclaw_solver<SOLVER, FZ>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, yL, yR, drytol, netL, netR, ms,
+                               fz);
     fL.h = netL[0];
     fL.s = ms;
     fR.h = netR[0];
@@ -848,12 +882,12 @@ __device__ __forceinline__ void lf_flux(double n1, double n2, const State& QL, c
 // One edge: dL/dR are the depths h - b of the two states, sqL/sqR their
 // sqrt(g * depth) and yL/yR RN(1 / depth) (only read for depths above the dry
 // tolerance).
-template <int SOLVER>
+template <int SOLVER, int FZ = 0>
 __device__ __forceinline__ void edge_flux(double n1, double n2, const State& QL, const State& QR, double dL,
                                           double dR, double sqL, double sqR, double yL, double yR, double drytol,
-                                          Update& fL, Update& fR, int axis = 0) {
+                                          Update& fL, Update& fR, int axis = 0, uint16_t* fz = nullptr) {
     if (SOLVER == FWAVE || SOLVER == AUG_RIEMANN)
-        geoclaw_flux<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, axis);
+        geoclaw_flux<SOLVER, FZ>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, axis, fz);
     else
         lf_flux<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, fL, fR, yL, yR);
 }

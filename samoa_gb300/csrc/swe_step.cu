@@ -388,6 +388,8 @@ int configure_launch(swe_ctx* c) {
         CUDA_TRY(cudaFuncSetAttribute(kernel_for(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
         CUDA_TRY(cudaFuncSetAttribute(fma_step_kernel(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
     }
+    CUDA_TRY(cudaFuncSetAttribute(step_kernel<FWAVE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    CUDA_TRY(cudaFuncSetAttribute(step_kernel<FWAVE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
     int per_sm = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, c->block_threads, c->smem));
     if (per_sm < 1)
@@ -579,8 +581,11 @@ int copy_state(swe_ctx* c, int to_device, double* h, double* hu, double* hv, dou
 
 // io: optional caller buffers {h, hu, hv, h_out, hu_out, hv_out} (device-accessible
 // addresses), b and flags: optional replacements of the context's arrays.
+// fz: 0 a plain step; 1 records every edge decision into erec (and the cells'
+// fixes into branch); 2 replays them (the f-wave only).
 int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double* const* io = nullptr,
-                 const double* b = nullptr, int8_t* flags = nullptr, int use_tma = 1) {
+                 const double* b = nullptr, int8_t* flags = nullptr, int use_tma = 1, int fz = 0,
+                 uint16_t* erec = nullptr) {
     StepArgs A;
     A.branch = branch;
     for (int k = 0; k < 2; ++k) {
@@ -627,6 +632,15 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     const bool fma = c->arith == SWE_ARITH_FMA && !branch;
     void* k = fma ? fma_step_kernel(c->params[0].solver) : (void*)kernel_for(c->params[0].solver);
     void* kx = fma ? fma_cross_kernel(c->params[0].solver) : cross_kernel_for(c->params[0].solver);
+    A.erec = erec;
+    A.xrec = erec ? erec + c->n_tasks : nullptr;
+    if (fz == 1) {
+        k = (void*)step_kernel<FWAVE, 1>;
+        kx = (void*)cross_edges_kernel<FWAVE, 1>;
+    } else if (fz == 2) {
+        k = (void*)step_kernel<FWAVE, 2>;
+        kx = (void*)cross_edges_kernel<FWAVE, 2>;
+    }
     const unsigned xblocks = pass ? (unsigned)((c->n_xtasks + 255) / 256) : 0u;
     void* args[] = {&A};
     for (int64_t s = 0; s < n_steps; ++s) {
@@ -1116,6 +1130,34 @@ int swe_traverse_gauges(swe_ctx* c, int64_t n_steps, int64_t n_gauges, const int
         gauge_kernel<<<blocks, 128, 0, c->stream>>>(c->gs, c->h[0], c->h[1], n_gauges, cells, c->mesh[0].n_cells,
                                                     out + (size_t)s * (size_t)n_gauges);
         CUDA_TRY(cudaGetLastError());
+    }
+    return SWE_OK;
+}
+
+int swe_traverse_frozen(swe_ctx* c, int64_t n_steps, int32_t mode, uint8_t* branch, int64_t branch_stride,
+                        uint16_t* edges, int64_t edge_stride, int64_t n_gauges, const int64_t* cells, double* out) {
+    int rc = ready(c);
+    if (rc) return rc;
+    if (n_inst(c) != 1) return set_error(SWE_E_INVALID, "branch-frozen runs are for single-instance contexts");
+    if (c->params[0].solver != SWE_SOLVER_FWAVE)
+        return set_error(SWE_E_INVALID, "branch-frozen runs support the f-wave solver");
+    if (mode != 1 && mode != 2) return set_error(SWE_E_INVALID, "mode %d (1 record, 2 replay)", mode);
+    if (n_steps < 0 || (n_steps > 0 && (!branch || !edges)) || branch_stride < c->cells_total ||
+        edge_stride < c->n_tasks + c->n_xtasks)
+        return set_error(SWE_E_INVALID, "bad record buffers (strides must be >= %lld cells, %lld edges)",
+                         (long long)c->cells_total, (long long)(c->n_tasks + c->n_xtasks));
+    if (n_gauges < 0 || (n_gauges > 0 && (!cells || !out))) return set_error(SWE_E_INVALID, "bad gauge arrays");
+    cudaSetDevice(c->device);
+    const int blocks = (int)std::min<int64_t>((n_gauges + 127) / 128, 1024);
+    for (int64_t s = 0; s < n_steps; ++s) {
+        if ((rc = launch_steps(c, 1, branch + s * branch_stride, nullptr, nullptr, nullptr, 1, mode,
+                               edges + s * edge_stride)))
+            return rc;
+        if (n_gauges > 0) {
+            gauge_kernel<<<blocks, 128, 0, c->stream>>>(c->gs, c->h[0], c->h[1], n_gauges, cells, c->mesh[0].n_cells,
+                                                        out + (size_t)s * (size_t)n_gauges);
+            CUDA_TRY(cudaGetLastError());
+        }
     }
     return SWE_OK;
 }
