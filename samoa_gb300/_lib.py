@@ -25,6 +25,7 @@ EXPORTS = [
     "swe_division_check", "swe_step_host", "swe_gauge_gradient",
     "swe_traverse_gauges", "swe_mesh_uniform_vertices", "swe_mesh_build", "swe_mesh_adapt",
     "swe_multiply_check", "swe_set_staging", "swe_get_task_counts", "swe_set_cross_pass", "swe_traverse_frozen",
+    "swe_set_segment_order",
 ]
 
 
@@ -73,6 +74,7 @@ def load():
         "swe_get_tiling": [P, P, P],
         "swe_get_task_counts": [P, P, P, P, P],
         "swe_set_cross_pass": [P, i32],
+        "swe_set_segment_order": [P, i32],
         "swe_traverse_frozen": [P, i64, i32, P, i64, P, i64, i64, P, P],
         "swe_mesh_uniform": [i32, P, P, P, P, P, P, P, P, P, P],
         "swe_mesh_validate": [i64, P, P, i64, P, P, i64, P, P],

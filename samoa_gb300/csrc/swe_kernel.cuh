@@ -55,6 +55,7 @@ struct StepArgs {
     const int4* tasks;
     const long long* seg_ptr;
     const int4* seg_info;      // {first cell, cells, instance, halo tasks at the end of its list}
+    const int32_t* seg_order;  // the order segments are handed out in (a permutation), or null: curve order
     const int4* xtasks;        // cross-segment edges (Task layout, pad = instance)
     double* xflux;             // [n_xtasks][cell a, cell b][h, hu, hv, max wave speed] of the current step
     long long n_xtasks;
@@ -331,8 +332,13 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     };
 
     // segments are handed out dynamically (CTAs that draw cheap segments, e.g.
-    // dry land, take more); each CTA still sees its segments in increasing order
-    if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+    // dry land, take more), in the order seg_order gives: spread over the
+    // domain, so that the CTAs an SM holds at one time mix wet and dry work
+    auto draw = [&]() {
+        const int k = (int)atomicAdd(&A.gs->next_seg, 1u);
+        s_seg = k < A.n_seg ? (A.seg_order ? __ldg(&A.seg_order[k]) : k) : A.n_seg;
+    };
+    if (tid == 0) draw();
     __syncthreads();
     int seg = s_seg;
     int kbuf = 0;
@@ -341,7 +347,7 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         int seg_next = A.n_seg;
         if (depth2) {  // draw and stage the next segment before working on this one
             __syncthreads();
-            if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+            if (tid == 0) draw();
             __syncthreads();
             seg_next = s_seg;
             if (seg_next < A.n_seg) issue(seg_next, kbuf ^ 1);
@@ -567,7 +573,7 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         }
         __syncthreads();
         if (!depth2) {  // draw and stage the next segment now
-            if (tid == 0) s_seg = (int)atomicAdd(&A.gs->next_seg, 1u);
+            if (tid == 0) draw();
             __syncthreads();
             seg_next = s_seg;
             if (seg_next < A.n_seg) issue(seg_next, 0);

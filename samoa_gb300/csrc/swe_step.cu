@@ -248,6 +248,7 @@ struct swe_ctx {
     int32_t stage_depth = 1;                        // segments staged ahead per CTA (1 or 2)
     int32_t arith = SWE_ARITH_STRICT;
     int32_t cross_mode = SWE_CROSS_AUTO;
+    int32_t seg_order_mode = SWE_ORDER_SPREAD;
     int64_t n_seg = 0, n_tasks = 0;
     int grid = 0, max_ndepth = 1;
     size_t smem = 0;
@@ -264,6 +265,7 @@ struct swe_ctx {
     int64_t n_xtasks = 0;
     long long* seg_ptr = nullptr;
     SegInfo* seg_info = nullptr;
+    int32_t* seg_order = nullptr;   // hand-out order of the segments (spread over each instance's domain)
     InstParams* ip = nullptr;
     InstScalars* is = nullptr;
     GlobalScalars* gs = nullptr;
@@ -314,9 +316,9 @@ void free_mesh_buffers(swe_ctx* c, bool release = true) {
         c->h[k] = c->hu[k] = c->hv[k] = nullptr;
     }
     cudaFree(c->b); cudaFree(c->depth); cudaFree(c->flags); cudaFree(c->tasks); cudaFree(c->seg_ptr);
-    cudaFree(c->seg_info); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->xtasks); cudaFree(c->xflux);
+    cudaFree(c->seg_info); cudaFree(c->seg_order); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->xtasks); cudaFree(c->xflux);
     c->b = nullptr; c->depth = nullptr; c->flags = nullptr; c->tasks = nullptr; c->seg_ptr = nullptr;
-    c->seg_info = nullptr; c->ip = nullptr; c->is = nullptr; c->xtasks = nullptr; c->xflux = nullptr;
+    c->seg_info = nullptr; c->seg_order = nullptr; c->ip = nullptr; c->is = nullptr; c->xtasks = nullptr; c->xflux = nullptr;
     c->n_xtasks = 0;
     c->cap_cells = c->cap_inst = c->cap_tasks = c->cap_segs = c->cap_xtasks = 0;
 }
@@ -401,6 +403,33 @@ int configure_launch(swe_ctx* c) {
     return SWE_OK;
 }
 
+// The order the step kernel hands segments out in: each instance's segments in
+// bit-reversed order of their index (the reversal over the next power of two,
+// skipping indices past the end), instances one after the other. The CTAs that
+// run at one time then work on segments spread over the instance's domain, so
+// an SM rarely holds only dry land (integer work, the FP64 pipe idle) or only
+// wet cells. Results do not depend on the order: the step's reductions are a
+// min, a max and an integer sum.
+static std::vector<int32_t> spread_order(const std::vector<SegInfo>& seg_info) {
+    std::vector<int32_t> order;
+    order.reserve(seg_info.size());
+    size_t s0 = 0;
+    while (s0 < seg_info.size()) {
+        size_t s1 = s0 + 1;
+        while (s1 < seg_info.size() && seg_info[s1].inst == seg_info[s0].inst) ++s1;
+        const uint64_t n = s1 - s0;
+        int bits = 0;
+        while (((uint64_t)1 << bits) < n) ++bits;
+        for (uint64_t k = 0; k < ((uint64_t)1 << bits); ++k) {
+            uint64_t r = 0;
+            for (int i = 0; i < bits; ++i) r |= ((k >> i) & 1u) << (bits - 1 - i);
+            if (r < n) order.push_back((int32_t)(s0 + r));
+        }
+        s0 = s1;
+    }
+    return order;
+}
+
 int rebuild_tasks(swe_ctx* c) {
     std::vector<int64_t> seg_ptr;
     std::vector<SegInfo> seg_info;
@@ -427,12 +456,15 @@ int rebuild_tasks(swe_ctx* c) {
     if (seg_info.size() + 1 > c->cap_segs) {
         cudaFree(c->seg_ptr);
         cudaFree(c->seg_info);
+        cudaFree(c->seg_order);
         c->seg_ptr = nullptr;
         c->seg_info = nullptr;
+        c->seg_order = nullptr;
         c->cap_segs = 0;
         const size_t cap = seg_info.size() + seg_info.size() / 8 + 16;
         if ((rc = device_alloc((void**)&c->seg_ptr, sizeof(long long) * (cap + 1)))) return rc;
         if ((rc = device_alloc((void**)&c->seg_info, sizeof(SegInfo) * cap))) return rc;
+        if ((rc = device_alloc((void**)&c->seg_order, sizeof(int32_t) * cap))) return rc;
         c->cap_segs = cap;
     }
     if (xtasks.size() > c->cap_xtasks) {
@@ -454,6 +486,10 @@ int rebuild_tasks(swe_ctx* c) {
                              c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->seg_info, seg_info.data(), sizeof(SegInfo) * seg_info.size(),
                              cudaMemcpyHostToDevice, c->stream));
+    const std::vector<int32_t> order = spread_order(seg_info);
+    if (order.size() != seg_info.size()) return set_error(SWE_E_INVALID, "segment order is not a permutation");
+    CUDA_TRY(cudaMemcpyAsync(c->seg_order, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice,
+                             c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     return configure_launch(c);
 }
@@ -599,6 +635,7 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     A.tasks = reinterpret_cast<const int4*>(c->tasks);
     A.seg_ptr = c->seg_ptr;
     A.seg_info = reinterpret_cast<const int4*>(c->seg_info);
+    A.seg_order = c->seg_order_mode == SWE_ORDER_SPREAD ? c->seg_order : nullptr;
     A.xtasks = reinterpret_cast<const int4*>(c->xtasks);
     A.xflux = c->xflux;
     A.n_xtasks = c->n_xtasks;
@@ -814,6 +851,14 @@ int swe_set_cross_pass(swe_ctx* c, int32_t mode) {
     if (!c) return set_error(SWE_E_INVALID, "null context");
     if (mode < SWE_CROSS_AUTO || mode > SWE_CROSS_INKERNEL) return set_error(SWE_E_INVALID, "cross mode %d", mode);
     c->cross_mode = mode;
+    drop_graphs(c);
+    return SWE_OK;
+}
+
+int swe_set_segment_order(swe_ctx* c, int32_t mode) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (mode != SWE_ORDER_CURVE && mode != SWE_ORDER_SPREAD) return set_error(SWE_E_INVALID, "segment order %d", mode);
+    c->seg_order_mode = mode;
     drop_graphs(c);
     return SWE_OK;
 }

@@ -103,10 +103,12 @@ def test_large_mesh_against_omp(swe_lib, oracle_lib):
         trav.close()
 
 
+@pytest.mark.parametrize("order", ["curve", "spread"])
 @pytest.mark.parametrize("mode", ["pass", "inkernel"])
-def test_cross_segment_modes_against_omp(swe_lib, oracle_lib, mode):
+def test_cross_segment_modes_against_omp(swe_lib, oracle_lib, mode, order):
     """Edges between two segments solved once by the pass before the step kernel,
-    or by both segments' CTAs: the same bits (state, flags, dt) as the oracle."""
+    or by both segments' CTAs, with segments handed out along the curve or
+    spread: the same bits (state, flags, dt) as the oracle."""
     scn = scenarios.ocean_basin(log2_cells=16, steps=4)
     g = scn.grid
     S = omp_state(g.mesh, g)
@@ -114,6 +116,7 @@ def test_cross_segment_modes_against_omp(swe_lib, oracle_lib, mode):
     trav = swe.SweEulerTimestepTraversal(scn.cfg)
     trav.set_tiling(256, 128)
     trav.ctx.set_cross_pass(mode)
+    trav.ctx.set_segment_order(order)
     try:
         for k in range(4):
             S.steps(P, 1)
