@@ -59,6 +59,6 @@ def random_states_scenario(solver, seed=5, depth=9):
     hu = rng.normal(0.0, 6.0, n) * d
     hv = rng.normal(0.0, 6.0, n) * d
     cfg = swe.Config(flux_solver=solver, boundary="outflow", courant_number=0.3, dry_tolerance=1e-3, scaling=1.0,
-                     offset=(-0.5, -0.5), i_min_depth=depth - 1, i_max_depth=depth + 1)
+                     offset=(-0.5, -0.5), i_min_depth=max(depth - 1, 0), i_max_depth=depth + 1)
     dt = swe.initial_dt(mesh, h, hu, hv, b, cfg.courant_number)
     return scenarios.Scenario("random", swe.Grid(mesh, h, hu, hv, b, 0.0, dt), cfg, 4)

@@ -6,13 +6,22 @@ import pytest
 
 from samoa_gb300 import scenarios, swe
 
-from .helpers import assert_state_equal, omp_state, oracle_params
+from .helpers import assert_state_equal, omp_state, oracle_params, random_states_scenario
 from .test_gpu_step import _odd_mesh
 
 pytestmark = pytest.mark.gpu
 
 
-def _ensemble_members():
+def _tiny_members():
+    """Instances of 2, 4 and 32 cells (random wet/dry states, f-wave)."""
+    out = []
+    for depth in (0, 1, 4):
+        scn = random_states_scenario("fwave", seed=11 + depth, depth=depth)
+        out.append((scn.grid.mesh, scn.grid, scn.cfg))
+    return out
+
+
+def _ensemble_members(tiny=False):
     members = []
     ens = scenarios.bowl_ensemble(n_instances=5, seed=9, log2_range=(8, 13))
     for m, g, c in zip(ens.meshes, ens.grids, ens.cfgs):
@@ -26,6 +35,9 @@ def _ensemble_members():
     cfg = base.cfg
     cfg.i_min_depth, cfg.i_max_depth = 3, 9
     members.insert(2, (odd, g, cfg))
+    if tiny:  # first, in the middle and last
+        t = _tiny_members()
+        members = [t[0]] + members[:3] + [t[1]] + members[3:] + [t[2]]
     return members
 
 
@@ -37,9 +49,10 @@ def _upload(ens, members):
     ens.set_times([g.r_time for _, g, _ in members], [g.r_dt for _, g, _ in members])
 
 
-@pytest.mark.parametrize("graph,staging", [(False, 1), (True, 1), (False, 2)])
-def test_ensemble_members_match_oracle(swe_lib, oracle_lib, graph, staging):
-    members = _ensemble_members()
+@pytest.mark.parametrize("graph,staging,tiny", [(False, 1, False), (True, 1, False), (False, 2, False),
+                                               (True, 1, True)])
+def test_ensemble_members_match_oracle(swe_lib, oracle_lib, graph, staging, tiny):
+    members = _ensemble_members(tiny)
     ens = swe.SweEnsemble(0)
     try:
         ens.set_tiling(128, 128)

@@ -12,7 +12,7 @@ import pytest
 from oracle import oracle as O
 from samoa_gb300 import scenarios, swe
 
-from .helpers import assert_state_equal, omp_state, oracle_params, walk_state
+from .helpers import assert_state_equal, omp_state, oracle_params, random_states_scenario, walk_state
 
 pytestmark = pytest.mark.gpu
 
@@ -303,6 +303,15 @@ def test_riemann_batch_against_oracle(swe_lib, oracle_lib):
         ok = np.isfinite(ol).all(1) & np.isfinite(orr).all(1)
         assert np.array_equal(gl[ok], ol[ok]) and np.array_equal(gr[ok], orr[ok]), solver
         assert np.array_equal(np.isfinite(gl).all(1) & np.isfinite(gr).all(1), ok), solver
+
+
+@pytest.mark.parametrize("depth", [0, 1, 2, 4])
+@pytest.mark.parametrize("solver", ["fwave", "aug_riemann", "llfbath"])
+def test_tiny_meshes_bitexact(swe_lib, oracle_lib, depth, solver):
+    """Meshes of 2 to 32 cells (one segment, no edges between segments, most
+    cells on the boundary): random wet/dry states, bit for bit against the walk."""
+    scn = random_states_scenario(solver, seed=7 + depth, depth=depth)
+    run_compare_walk(scn, 6)
 
 
 def test_tiling_limits(swe_lib):
