@@ -461,12 +461,39 @@ def adjoint_windowed(a, case, device):
         fd = (W.objective(case["h0"] + eps * dd, case["b"]) - W.objective(case["h0"] - eps * dd, case["b"])) / (2 * eps)
         ad = float(gh @ dd)
         errs.append(abs(fd - ad) / max(abs(ad), 1e-300))
+    # branch-frozen J: every window's decisions recorded once, then replayed
+    ferrs, fb, fbr = [], None, []
+    if a.adjoint_fd_frozen:
+        Jrec = W.objective_frozen(case["h0"], case["b"], record=True)
+        assert Jrec == J, (Jrec, J)
+        for _ in range(a.adjoint_fd_frozen):
+            dd = rng.normal(size=mesh.n_cells)
+            eps = 1e-4 * float(np.abs(case["h0"]).max())
+            Jf = lambda s_: W.objective_frozen(case["h0"] + s_ * eps * dd, case["b"], record=False)
+            fd = (8.0 * (Jf(1) - Jf(-1)) - (Jf(2) - Jf(-2))) / (12.0 * eps)
+            ad = float(gh @ dd)
+            ferrs.append(abs(fd - ad) / max(abs(ad), 1e-300))
+        eps = 1e-4 * float(np.abs(case["b"]).max())
+        for k in range(5):  # b along its gradient, then random directions (error against |g| |d|)
+            dd = gb / np.linalg.norm(gb) if k == 0 else rng.normal(size=mesh.n_cells)
+            Jf = lambda s_: W.objective_frozen(case["h0"], case["b"] + s_ * eps * dd, record=False)
+            fd = (8.0 * (Jf(1) - Jf(-1)) - (Jf(2) - Jf(-2))) / (12.0 * eps)
+            ad = float(gb @ dd)
+            if k == 0:
+                fb = abs(fd - ad) / abs(ad)
+            else:
+                fbr.append(abs(fd - ad) / (np.linalg.norm(gb) * np.linalg.norm(dd)))
     cells = W.stats["cells"]
     return {"window": 50, "windows": len(cells), "depths": [d - 2, d + 1], "cells_first": cells[0],
             "cells_min": min(cells), "cells_max": max(cells), "J": J, "forward_s": t_fwd, "gradient_s": t_grad,
             "gradient_over_forward": t_grad / t_fwd, "fd_directions_h0": len(errs), "fd_max_rel_err_h0": max(errs),
+            "fd_frozen_directions_h0": len(ferrs), "fd_frozen_max_rel_err_h0": max(ferrs, default=None),
+            "fd_frozen_rel_err_b_along_gradient": fb, "fd_frozen_directions_b": len(fbr),
+            "fd_frozen_max_err_over_grad_norm_b": max(fbr, default=None),
             "note": "gradient_s and forward_s include the host work between windows (mesh upload, transfer, "
-                    "gauge location); the forward run that fixes the mesh sequence is not timed"}
+                    "gauge location); the forward run that fixes the mesh sequence is not timed; fd_*: plain "
+                    "central differences (eps 1e-6 relative, deep cells), branch-limited like the uniform mesh's; "
+                    "fd_frozen_*: 4-point differences of the branch-frozen J (eps 1e-4 relative, all cells)"}
 
 
 def run_gpu(a, rank, world, local):

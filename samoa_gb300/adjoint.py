@@ -404,10 +404,14 @@ class WindowedGaugeProblem:
     def _windows(self):
         return [(k, min(k + self.window, self.T)) for k in range(0, self.T, self.window)]
 
-    def _forward(self, h0, b0, record_plan):
+    def _forward(self, h0, b0, record_plan, frozen=None):
         """Run all windows from (h0, b0) at rest; returns J, the initial states of
-        the windows and (first run) the meshes, gauges and transfers."""
+        the windows and (first run) the meshes, gauges and transfers. frozen:
+        None (plain steps), "record" (branch-frozen runs recording every window's
+        decisions) or "replay" (taking them from the last recording)."""
         from .swe import adapt
+        if frozen == "record":
+            self.frozen = []
         ctx = SweContext(self.device)
         try:
             ctx.set_params(self.params)
@@ -432,7 +436,21 @@ class WindowedGaugeProblem:
                 dev = torch.device("cuda", self.device)
                 gi = torch.as_tensor(gw, dtype=torch.int64, device=dev)
                 gv = torch.empty((t1 - t0, len(gw)), dtype=torch.float64, device=dev)
-                _lib.check(ctx.L.swe_traverse_gauges(ctx.ptr, t1 - t0, len(gw), _vp(gi), _vp(gv)))
+                if frozen is None:
+                    _lib.check(ctx.L.swe_traverse_gauges(ctx.ptr, t1 - t0, len(gw), _vp(gi), _vp(gv)))
+                else:
+                    counts = ctx.task_counts()
+                    es = counts["tasks"] + counts["cross_edges"]
+                    stride = (mesh.n_cells + 1) & ~1
+                    if frozen == "record":
+                        self.frozen.append((torch.empty((t1 - t0, stride), dtype=torch.uint8, device=dev),
+                                            torch.empty((t1 - t0, es), dtype=torch.int16, device=dev)))
+                    br, ed = self.frozen[w]
+                    if ed.shape[1] != es:
+                        raise ValueError("the recording belongs to another mesh")
+                    torch.cuda.synchronize(dev)
+                    _lib.check(ctx.L.swe_traverse_frozen(ctx.ptr, t1 - t0, 1 if frozen == "record" else 2, _vp(br),
+                                                         stride, _vp(ed), es, len(gw), _vp(gi), _vp(gv)))
                 ctx.synchronize()
                 J += float(((gv.cpu().numpy() - self.obs[t0:t1]) ** 2).sum())
                 h, hu, hv, _ = ctx.download_state()
@@ -455,6 +473,20 @@ class WindowedGaugeProblem:
 
     def objective(self, h0, b0):
         J, _ = self._forward(h0, b0, self.plan is None)
+        return J
+
+    def objective_frozen(self, h0, b0, record):
+        """J with the plan's meshes and transfers and, in every window, every
+        branch decision of the f-wave step taken from a recorded run
+        (swe_traverse_frozen): record=True runs from (h0, b0) and records,
+        record=False replays the last recording. Near the recorded run J is then
+        smooth, so its finite differences check the adjoint without crossing a
+        kink. The plan is fixed first if no run has fixed it."""
+        if self.plan is None:
+            self._forward(h0, b0, True)
+        if not record and getattr(self, "frozen", None) is None:
+            raise ValueError("record a branch-frozen run first")
+        J, _ = self._forward(h0, b0, False, frozen="record" if record else "replay")
         return J
 
     def gradient(self, h0, b0):
