@@ -140,7 +140,9 @@ int swe_last_error(char* buf, size_t n);
  * memory per cell, 22 with staging depth 2, at most 227 KB in all) and threads
  * per block (multiple of 32, 64..256); 0 keeps
  * the current value. A mesh upload or
- * this call rebuilds the segment task lists. */
+ * this call rebuilds the segment task lists. Until a segment length is set
+ * here, each mesh upload picks it by size: 512 cells from 2^20 cells on, 256
+ * below (more segments than resident CTAs on small meshes). */
 int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
 
 /* Staging depth of the step kernel: 1 = a CTA stages a segment's state into

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "swe_internal.h"
@@ -244,7 +245,13 @@ struct swe_ctx {
     int64_t cells_packed = 0;      // sum of the instances' cells (host layout)
     bool has_mesh = false, has_state = false;
     // tiling
-    int32_t seg_cells = 512, block_threads = 128;  // the best of a sweep on GB300 (2^24 cells)
+    // 512 x 128: the best of a sweep on GB300 (2^22..2^26 cells). Until the caller
+    // sets a tiling, meshes below 2^20 cells get 256-cell segments: with 512 a
+    // 2^18-cell mesh has 512 segments for ~456 resident CTAs, and a step takes
+    // two segment-times (measured at 2^18: forward step 0.170 -> 0.145 ms,
+    // adjoint step 0.242 -> 0.222 ms).
+    int32_t seg_cells = 512, block_threads = 128;
+    bool tiling_set = false;
     int32_t stage_depth = 1;                        // segments staged ahead per CTA (1 or 2)
     int32_t arith = SWE_ARITH_STRICT;
     int32_t cross_mode = SWE_CROSS_AUTO;
@@ -382,16 +389,33 @@ int upload_inst_params(swe_ctx* c) {
     return SWE_OK;
 }
 
+// A kernel's dynamic shared-memory limit is an attribute of the function, shared
+// by every context of the process: contexts with different tilings only ever
+// raise it (the limit does not change the resources of a launch that asks for
+// less), so a context never finds it lowered by another.
+int raise_smem_limit(const void* k, size_t bytes) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    cudaFuncAttributes fa;
+    CUDA_TRY(cudaFuncGetAttributes(&fa, k));
+    if ((size_t)fa.maxDynamicSharedSizeBytes < bytes)
+        CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    return SWE_OK;
+}
+
 int configure_launch(swe_ctx* c) {
     c->smem = smem_bytes(c);
     StepKernel k = kernel_for(c->params.empty() ? FWAVE : c->params[0].solver);
     if (!k) return set_error(SWE_E_INVALID, "unknown solver");
+    int rc;
     for (int s : {FWAVE, AUG_RIEMANN, LF, LF_BATH, LLF, LLF_BATH}) {
-        CUDA_TRY(cudaFuncSetAttribute(kernel_for(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
-        CUDA_TRY(cudaFuncSetAttribute(fma_step_kernel(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+        if ((rc = raise_smem_limit((const void*)kernel_for(s), c->smem)) ||
+            (rc = raise_smem_limit((const void*)fma_step_kernel(s), c->smem)))
+            return rc;
     }
-    CUDA_TRY(cudaFuncSetAttribute(step_kernel<FWAVE, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
-    CUDA_TRY(cudaFuncSetAttribute(step_kernel<FWAVE, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    if ((rc = raise_smem_limit((const void*)step_kernel<FWAVE, 1>, c->smem)) ||
+        (rc = raise_smem_limit((const void*)step_kernel<FWAVE, 2>, c->smem)))
+        return rc;
     int per_sm = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, c->block_threads, c->smem));
     if (per_sm < 1)
@@ -545,6 +569,7 @@ int upload_meshes(swe_ctx* c, int64_t ni, const int64_t* n_cells, const int64_t*
     c->offset.swap(offset);
     c->cells_total = off;
     c->cells_packed = pc;
+    if (!c->tiling_set) c->seg_cells = off < ((int64_t)1 << 20) ? 256 : 512;
     c->max_ndepth = max_nd;
     swe_params p0 = c->params.empty() ? swe_params{} : c->params[0];
     c->params.assign((size_t)ni, p0);
@@ -813,7 +838,10 @@ int swe_set_tiling(swe_ctx* c, int32_t seg_cells, int32_t block_threads) {
     if (seg_cells && smem_bytes_for(seg_cells, c->stage_depth, kMaxDepth + 1) > kMaxSmem)
         return set_error(SWE_E_INVALID, "segment_cells %d with staging depth %d exceeds shared memory", seg_cells,
                          c->stage_depth);
-    if (seg_cells) c->seg_cells = seg_cells;
+    if (seg_cells) {
+        c->seg_cells = seg_cells;
+        c->tiling_set = true;
+    }
     if (block_threads) c->block_threads = block_threads;
     if (!c->has_mesh) return SWE_OK;
     cudaSetDevice(c->device);
@@ -1284,7 +1312,7 @@ int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double*
     const AdjKernel kern = adjoint_kernel_for(solver);
     if (!kern) return set_error(SWE_E_INVALID, "the adjoint differentiates the f-wave, augmented and Lax-Friedrichs fluxes");
     if (c->adj_seg_cells != c->seg_cells || c->adj_solver != solver) {
-        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (int rc = raise_smem_limit((const void*)kern, smem)) return rc;
         int per_sm = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
         if (per_sm < 1) return set_error(SWE_E_INVALID, "adjoint tiling does not fit an SM");

@@ -314,6 +314,27 @@ def test_tiny_meshes_bitexact(swe_lib, oracle_lib, depth, solver):
     run_compare_walk(scn, 6)
 
 
+def test_contexts_with_different_tilings_interleave(swe_lib, oracle_lib):
+    """Two contexts of one process with different segment lengths, stepped in
+    turns (a kernel's shared-memory limit is an attribute of the function, not
+    of a context): both run and match the oracle bit for bit."""
+    scns = [scenarios.radial_dam_break(log2_cells=12, boundary="slip"),
+            scenarios.parabolic_bowl(log2_cells=12, solver="fwave", amplitude=2.0, sigma=0.08)]
+    travs = [swe.SweEulerTimestepTraversal(s.cfg) for s in scns]
+    try:
+        travs[0].set_tiling(1024, 256)
+        travs[1].set_tiling(128, 128)
+        refs = [(omp_state(s.grid.mesh, s.grid), oracle_params(s.cfg)) for s in scns]
+        for k in range(3):
+            for s, t, (S, P) in zip(scns, travs, refs):
+                S.steps(P, 1)
+                t.traverse(s.grid)
+                assert_state_equal("%s step %d" % (s.name, k), s.grid.h, s.grid.hu, s.grid.hv, S.h, S.hu, S.hv)
+    finally:
+        for t in travs:
+            t.close()
+
+
 def test_tiling_limits(swe_lib):
     scn = scenarios.radial_dam_break(log2_cells=8)
     trav = swe.SweEulerTimestepTraversal(scn.cfg)
