@@ -85,6 +85,21 @@ def adaptive_dam_break(min_depth=6, max_depth=12, solver="fwave", boundary="outf
     return Scenario("adaptive_dam_break", _grid(mesh, cfg, surface(x, y), b), cfg, 50)
 
 
+def ci_dam_break(solver="llfbath", min_depth=0, max_depth=8):
+    """The reference's own smoke run (.travis.yml:28-37: `-dmax 8 -nmax 10` with
+    llfbath or aug_riemann): the default SWE scenario without ASAGI, i.e. the
+    domain [-5, 5]^2 (scaling 10, src/SWE/SWE.f90:169-170), bathymetry 0
+    (src/SWE/SWE_initialize.f90:186), surface 1 m for x < 0 and 0 m elsewhere
+    (:349-370: dry land on the right), at rest; depths 0..8, Courant 0.45, dry
+    tolerance 0.01 (src/Config.f90:183), a-priori refinement along the step."""
+    cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=0.01, scaling=10.0,
+                 offset=(-5.0, -5.0), i_min_depth=min_depth, i_max_depth=max_depth)
+    surface = lambda x, y: np.where(x < 0.0, 1.0, 0.0)
+    mesh = apriori_mesh(cfg, surface)
+    x, y = _world(mesh, cfg)
+    return Scenario("ci_dam_break", _grid(mesh, cfg, surface(x, y), np.zeros(mesh.n_cells)), cfg, 10)
+
+
 def bowl_bathymetry(x, y, h0=10.0, a=0.4):
     r2 = x * x + y * y
     return -h0 * (1.0 - r2 / (a * a))
