@@ -113,6 +113,10 @@ def test_null_arguments_are_errors(swe_lib):
     assert swe_lib.swe_traverse(None, 1) == -1
     assert swe_lib.swe_set_params(None, None) == -1
     assert swe_lib.swe_destroy(None) == 0
+    # tuning calls on a null context report an error instead of touching memory
+    assert swe_lib.swe_set_segment_order(None, 1) == -1
+    assert swe_lib.swe_set_cross_pass(None, 0) == -1
+    assert swe_lib.swe_set_tiling(None, 512, 128) == -1
     buf = C.create_string_buffer(8)
     assert swe_lib.swe_last_error(buf, 8) == 0
 
