@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--adaptive-steps", type=int, default=20)
     ap.add_argument("--tune-log2-cells", type=int, default=22)
     ap.add_argument("--cpu-sample-log2", type=int, default=22)
-    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--cpu-steps", type=int, default=500,
+                    help="steps of the CPU baseline on its sample (500 x 2^22 cells: ~10 s on 16 Grace cores)")
     ap.add_argument("--segment-cells", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
     ap.add_argument("--arith", default="strict", choices=["strict", "fma"])
