@@ -176,12 +176,14 @@ int swe_get_tiling(swe_ctx* ctx, int32_t* segment_cells, int32_t* block_threads)
 int swe_set_cross_pass(swe_ctx* ctx, int32_t mode);
 
 /* The order the step kernel hands its segments out in. CURVE: along the
- * space-filling curve. SPREAD (the default): each instance's segments in
- * bit-reversed index order, so that the CTAs working at one time hold segments
- * from all over the domain and mix cheap (dry) and FP64-heavy (wet) work. The
- * results are bit identical. No reference counterpart. */
+ * space-filling curve. SPREAD: each instance's segments in bit-reversed index
+ * order, so that the CTAs working at one time hold segments from all over the
+ * domain and mix cheap (dry) and FP64-heavy (wet) work. AUTO (the default):
+ * SPREAD from 2048 segments on, CURVE below. The results are bit identical.
+ * No reference counterpart. */
 #define SWE_ORDER_CURVE 0
 #define SWE_ORDER_SPREAD 1
+#define SWE_ORDER_AUTO 2
 int swe_set_segment_order(swe_ctx* ctx, int32_t mode);
 
 /* Sizes of the uploaded mesh's work lists: segments, edge tasks in the segment

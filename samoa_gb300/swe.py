@@ -200,9 +200,10 @@ class SweContext:
         _lib.check(self.L.swe_set_cross_pass(self.ptr, {"auto": 0, "pass": 1, "inkernel": 2}[mode]))
 
     def set_segment_order(self, mode):
-        """The order segments are handed out in: "spread" (default; bit-reversed within each
-        instance, mixing wet and dry work on every SM) or "curve"; bit-identical results."""
-        _lib.check(self.L.swe_set_segment_order(self.ptr, {"curve": 0, "spread": 1}[mode]))
+        """The order segments are handed out in: "spread" (bit-reversed within each instance,
+        mixing wet and dry work on every SM), "curve", or "auto" (default: spread from 2048
+        segments on); bit-identical results."""
+        _lib.check(self.L.swe_set_segment_order(self.ptr, {"curve": 0, "spread": 1, "auto": 2}[mode]))
 
     def task_counts(self):
         """Segments, edge tasks, edges between two segments and kernel launches per step

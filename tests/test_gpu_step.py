@@ -103,7 +103,7 @@ def test_large_mesh_against_omp(swe_lib, oracle_lib):
         trav.close()
 
 
-@pytest.mark.parametrize("order", ["curve", "spread"])
+@pytest.mark.parametrize("order", ["curve", "spread", "auto"])
 @pytest.mark.parametrize("mode", ["pass", "inkernel"])
 def test_cross_segment_modes_against_omp(swe_lib, oracle_lib, mode, order):
     """Edges between two segments solved once by the pass before the step kernel,
