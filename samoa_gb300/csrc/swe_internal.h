@@ -3,6 +3,10 @@
 
 #include <stdint.h>
 
+#include <algorithm>
+#include <memory>
+#include <thread>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -68,15 +72,68 @@ struct GlobalScalars {
 };
 
 // Mesh as ingested from the C ABI (validated, a < b on inner edges).
+// std::vector storage whose resize leaves new elements default-initialised (no
+// zeroing pass): large host arrays are first written, page by page, by the
+// threads that fill them.
+template <class T>
+struct NoInit : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInit<U>;
+    };
+    NoInit() = default;
+    template <class U>
+    NoInit(const NoInit<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+        ::new ((void*)p) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new ((void*)p) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using hvec = std::vector<T, NoInit<T>>;
+
 struct HostMesh {
     int64_t n_cells = 0, n_edges = 0, n_bnd = 0;
     int min_depth = 0, max_depth = 0;
     std::vector<int8_t> depth, plotter;
-    std::vector<int64_t> ea, eb, bc;
-    std::vector<int8_t> la, lb, bl;
+    hvec<int64_t> ea, eb, bc;
+    hvec<int8_t> la, lb, bl;
 };
 
 int set_error(int code, const char* fmt, ...);
+
+// Host passes over large meshes run on several threads: [0, n) is split into
+// `parts` contiguous ranges, fn(begin, end, part) runs each (part 0 on the
+// calling thread). Meshes below 2^18 items stay on one thread.
+#ifndef SWE_HOST_THREADS
+#define SWE_HOST_THREADS 16
+#endif
+inline int host_parts(int64_t n) {
+    if (n < ((int64_t)1 << 18)) return 1;
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    return (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)std::min(hw, SWE_HOST_THREADS), n >> 16}));
+}
+template <class F>
+void parallel_parts(int64_t n, int parts, F&& fn) {
+    auto range = [&](int p, int64_t& b, int64_t& e) {
+        b = n * p / parts;
+        e = n * (p + 1) / parts;
+    };
+    std::vector<std::thread> th;
+    for (int p = 1; p < parts; ++p) {
+        int64_t b, e;
+        range(p, b, e);
+        th.emplace_back([&fn, b, e, p] { fn(b, e, p); });
+    }
+    int64_t b, e;
+    range(0, b, e);
+    fn(b, e, 0);
+    for (auto& t : th) t.join();
+}
 
 // A mesh built by the Sierpinski walk from its leaf depths (swe_mesh.cpp).
 struct BuiltMesh {
@@ -122,7 +179,7 @@ struct alignas(16) SegInfo {
 // Edge tasks of one instance's segments (appended to seg_ptr / seg_info /
 // tasks) and its cross-segment edges (appended to xtasks).
 int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t seg_cells, std::vector<int64_t>& seg_ptr,
-                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks, std::vector<Task>& xtasks);
+                std::vector<SegInfo>& seg_info, hvec<Task>& tasks, hvec<Task>& xtasks);
 
 // Geometry tables restating src/SFC_data_types.f90:509-700 (host side, exact).
 void geometry_tables(double leg[kMaxDepth + 2], double vol[kMaxDepth + 1], double normal[17][3][2]);

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 namespace swe {
@@ -288,88 +289,139 @@ static int normal_axis(int p, int k) {
 // flux's rotation), then the halo tasks, each class in input order (boundary
 // edges, then inner edges). Placed by counting, no sort.
 int build_tasks(const HostMesh& m, int64_t offset, int32_t inst, int32_t T, std::vector<int64_t>& seg_ptr,
-                std::vector<SegInfo>& seg_info, std::vector<Task>& tasks, std::vector<Task>& xtasks) {
+                std::vector<SegInfo>& seg_info, hvec<Task>& tasks, hvec<Task>& xtasks) {
     const int64_t n = m.n_cells;
     const int64_t nseg = (n + T - 1) / T;
     if (seg_ptr.empty()) seg_ptr.push_back(0);
-    const size_t s0 = seg_info.size();
     // task kinds: boundary edges and the inner edges inside one segment are class 0
     // (diagonal) or 1 (axis-aligned); an inner edge between two segments is class 2
-    // (a halo task) in both
-    std::vector<int8_t> bnd_axis((size_t)m.n_bnd), edge_axis((size_t)m.n_edges);
-    std::vector<int64_t> cnt((size_t)(3 * nseg), 0);
-    for (int64_t j = 0; j < m.n_bnd; ++j) {
-        const int64_t c = m.bc[(size_t)j];
-        bnd_axis[(size_t)j] = (int8_t)normal_axis(m.plotter[(size_t)c], m.bl[(size_t)j] - 1);
-        cnt[(size_t)(3 * (c / T) + (bnd_axis[(size_t)j] ? 1 : 0))]++;
-    }
-    for (int64_t e = 0; e < m.n_edges; ++e) {
-        const int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
-        edge_axis[(size_t)e] = (int8_t)normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1);
-        const int64_t sa = a / T, sb = b / T;
-        if (sa == sb) {
-            cnt[(size_t)(3 * sa + (edge_axis[(size_t)e] ? 1 : 0))]++;
-        } else {
-            cnt[(size_t)(3 * sa + 2)]++;
-            cnt[(size_t)(3 * sb + 2)]++;
+    // (a halo task) in both. Counted per part of the boundary and edge lists, then
+    // placed in list order (boundary edges first, then inner edges; cross edges
+    // numbered in edge order), so the lists do not depend on the number of parts.
+    const int PB = host_parts(m.n_bnd), PE = host_parts(m.n_edges);
+    const size_t ns = (size_t)(3 * nseg);
+    std::vector<std::vector<int64_t>> cb((size_t)PB), ce((size_t)PE);
+    std::vector<int64_t> xc((size_t)PE, 0);
+    parallel_parts(m.n_bnd, PB, [&](int64_t j0, int64_t j1, int p) {
+        std::vector<int64_t>& c = cb[(size_t)p];
+        c.assign(ns, 0);
+        for (int64_t j = j0; j < j1; ++j) {
+            const int64_t cell = m.bc[(size_t)j];
+            const int ax = normal_axis(m.plotter[(size_t)cell], m.bl[(size_t)j] - 1);
+            c[(size_t)(3 * (cell / T) + (ax ? 1 : 0))]++;
         }
-    }
+    });
+    parallel_parts(m.n_edges, PE, [&](int64_t e0, int64_t e1, int p) {
+        std::vector<int64_t>& c = ce[(size_t)p];
+        c.assign(ns, 0);
+        int64_t x = 0;
+        for (int64_t e = e0; e < e1; ++e) {
+            const int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
+            const int64_t sa = a / T, sb = b / T;
+            if (sa == sb) {
+                const int ax = normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1);
+                c[(size_t)(3 * sa + (ax ? 1 : 0))]++;
+            } else {
+                c[(size_t)(3 * sa + 2)]++;
+                c[(size_t)(3 * sb + 2)]++;
+                ++x;
+            }
+        }
+        xc[(size_t)p] = x;
+    });
+    // slot starts: segments in order, classes 0, 1, 2 within a segment
     const int64_t base = seg_ptr.back();
-    std::vector<int64_t> fill((size_t)(3 * nseg));
+    std::vector<int64_t> fill(ns);
     int64_t pos = base;
     for (int64_t sg = 0; sg < nseg; ++sg) {
         for (int k = 0; k < 3; ++k) {
-            fill[(size_t)(3 * sg + k)] = pos;
-            pos += cnt[(size_t)(3 * sg + k)];
+            const size_t sl = (size_t)(3 * sg + k);
+            fill[sl] = pos;
+            int64_t cnt = 0;
+            for (int p = 0; p < PB; ++p) cnt += cb[(size_t)p][sl];
+            for (int p = 0; p < PE; ++p) cnt += ce[(size_t)p][sl];
+            pos += cnt;
+            if (k == 2) {
+                SegInfo si;
+                si.c0 = (int32_t)(offset + sg * T);
+                si.cn = (int32_t)std::min<int64_t>(T, n - sg * T);
+                si.inst = inst;
+                si.halo = (int32_t)cnt;
+                seg_info.push_back(si);
+            }
         }
         seg_ptr.push_back(pos);
-        SegInfo si;
-        si.c0 = (int32_t)(offset + sg * T);
-        si.cn = (int32_t)std::min<int64_t>(T, n - sg * T);
-        si.inst = inst;
-        si.halo = (int32_t)cnt[(size_t)(3 * sg + 2)];
-        seg_info.push_back(si);
     }
-    (void)s0;
-    tasks.resize((size_t)pos);
-    for (int64_t j = 0; j < m.n_bnd; ++j) {
-        const int64_t c = m.bc[(size_t)j];
-        Task t;
-        t.a = (int32_t)(offset + c);
-        t.b = -1;
-        t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true, bnd_axis[(size_t)j]);
-        t.pad = 0;
-        tasks[(size_t)fill[(size_t)(3 * (c / T) + (bnd_axis[(size_t)j] ? 1 : 0))]++] = t;
-    }
-    for (int64_t e = 0; e < m.n_edges; ++e) {
-        const int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
-        Task t;
-        t.a = (int32_t)(offset + a);
-        t.b = (int32_t)(offset + b);
-        t.meta = pack_meta(m.la[(size_t)e] - 1, m.lb[(size_t)e] - 1, m.plotter[(size_t)a], m.plotter[(size_t)b], false,
-                           edge_axis[(size_t)e]);
-        t.pad = 0;
-        const int64_t sa = a / T, sb = b / T;
-        if (sb == sa) {
-            tasks[(size_t)fill[(size_t)(3 * sa + (edge_axis[(size_t)e] ? 1 : 0))]++] = t;
-            continue;
+    // each part's first position per slot (turn the counts into running starts)
+    for (size_t sl = 0; sl < ns; ++sl) {
+        int64_t at = fill[sl];
+        for (int p = 0; p < PB; ++p) {
+            const int64_t c = cb[(size_t)p][sl];
+            cb[(size_t)p][sl] = at;
+            at += c;
         }
-        // an edge between two segments: computed once by the cross-edge pass,
-        // each segment copies its own side's update
-        if (xtasks.size() >= ((size_t)1 << 31)) return set_error(SWE_E_INVALID, "too many cross-segment edges");
-        Task h = t;
-        h.meta |= kHaloBit;
-        h.pad = (uint32_t)xtasks.size();
-        t.pad = (uint32_t)inst;
-        xtasks.push_back(t);
-        tasks[(size_t)fill[(size_t)(3 * sa + 2)]++] = h;
-        tasks[(size_t)fill[(size_t)(3 * sb + 2)]++] = h;
+        for (int p = 0; p < PE; ++p) {
+            const int64_t c = ce[(size_t)p][sl];
+            ce[(size_t)p][sl] = at;
+            at += c;
+        }
     }
+    int64_t nx = (int64_t)xtasks.size();
+    for (int p = 0; p < PE; ++p) {
+        const int64_t c = xc[(size_t)p];
+        xc[(size_t)p] = nx;
+        nx += c;
+    }
+    if (nx > ((int64_t)1 << 31)) return set_error(SWE_E_INVALID, "too many cross-segment edges");
+    tasks.resize((size_t)pos);
+    xtasks.resize((size_t)nx);
+    parallel_parts(m.n_bnd, PB, [&](int64_t j0, int64_t j1, int p) {
+        std::vector<int64_t>& at = cb[(size_t)p];
+        for (int64_t j = j0; j < j1; ++j) {
+            const int64_t c = m.bc[(size_t)j];
+            const int ax = normal_axis(m.plotter[(size_t)c], m.bl[(size_t)j] - 1);
+            Task t;
+            t.a = (int32_t)(offset + c);
+            t.b = -1;
+            t.meta = pack_meta(m.bl[(size_t)j] - 1, 0, m.plotter[(size_t)c], 1, true, ax);
+            t.pad = 0;
+            tasks[(size_t)at[(size_t)(3 * (c / T) + (ax ? 1 : 0))]++] = t;
+        }
+    });
+    parallel_parts(m.n_edges, PE, [&](int64_t e0, int64_t e1, int p) {
+        std::vector<int64_t>& at = ce[(size_t)p];
+        int64_t xi = xc[(size_t)p];
+        for (int64_t e = e0; e < e1; ++e) {
+            const int64_t a = m.ea[(size_t)e], b = m.eb[(size_t)e];
+            const int ax = normal_axis(m.plotter[(size_t)a], m.la[(size_t)e] - 1);
+            Task t;
+            t.a = (int32_t)(offset + a);
+            t.b = (int32_t)(offset + b);
+            t.meta = pack_meta(m.la[(size_t)e] - 1, m.lb[(size_t)e] - 1, m.plotter[(size_t)a], m.plotter[(size_t)b],
+                               false, ax);
+            t.pad = 0;
+            const int64_t sa = a / T, sb = b / T;
+            if (sb == sa) {
+                tasks[(size_t)at[(size_t)(3 * sa + (ax ? 1 : 0))]++] = t;
+                continue;
+            }
+            // an edge between two segments: computed once by the cross-edge pass,
+            // each segment copies its own side's update
+            Task h = t;
+            h.meta |= kHaloBit;
+            h.pad = (uint32_t)xi;
+            t.pad = (uint32_t)inst;
+            xtasks[(size_t)xi++] = t;
+            tasks[(size_t)at[(size_t)(3 * sa + 2)]++] = h;
+            tasks[(size_t)at[(size_t)(3 * sb + 2)]++] = h;
+        }
+    });
     return SWE_OK;
 }
 
-// Validate a mesh given through the C ABI and store it with a < b per edge.
-int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
+// Validate a mesh given through the C ABI and store it with a < b per edge, one
+// item after the other: the first bad item in list order is the one reported.
+static int ingest_serial(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
                 const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
                 const int8_t* bnd_local) {
     if (n_cells <= 0 || n_cells >= ((int64_t)1 << 31) - 1)
@@ -436,6 +488,120 @@ int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t*
         m.bl[(size_t)j] = (int8_t)l;
     }
     // 2*n_edges + n_bnd == 3*n_cells and no slot claimed twice => every slot used once
+    return SWE_OK;
+}
+
+// Validate a mesh given through the C ABI and store it with a < b per edge. A
+// large mesh is checked in parts on host threads without atomics: every claim
+// of a (cell, local edge) slot writes its edge number into the slot, and a
+// second pass checks that each claim still owns its slot (of two claims of one
+// slot one loses). With 2 n_edges + n_bnd = 3 n_cells and no slot claimed
+// twice, every slot is used once. On any failure the serial check runs again
+// and reports the first bad item in list order.
+int ingest_mesh(HostMesh& m, int64_t n_cells, const int8_t* depth, const int8_t* plotter, int64_t n_edges,
+                const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd, const int64_t* bnd_cell,
+                const int8_t* bnd_local) {
+    const int PE = host_parts(n_edges);
+    if (PE == 1 || n_cells <= 0 || n_cells >= ((int64_t)1 << 30) || n_edges < 0 || n_bnd < 0 ||
+        2 * n_edges + n_bnd != 3 * n_cells || !depth || !plotter || !edge_cells || !edge_local ||
+        (n_bnd && (!bnd_cell || !bnd_local)))
+        return ingest_serial(m, n_cells, depth, plotter, n_edges, edge_cells, edge_local, n_bnd, bnd_cell, bnd_local);
+    m.n_cells = n_cells;
+    m.n_edges = n_edges;
+    m.n_bnd = n_bnd;
+    m.depth.assign(depth, depth + n_cells);
+    m.plotter.assign(plotter, plotter + n_cells);
+    const int PC = host_parts(n_cells), PB = host_parts(n_bnd);
+    std::vector<int> pmin((size_t)PC, 127), pmax((size_t)PC, -1);
+    std::vector<uint8_t> ok((size_t)std::max({PC, PE, PB}), 1);
+    parallel_parts(n_cells, PC, [&](int64_t c0, int64_t c1, int p) {
+        int lo = 127, hi = -1;
+        for (int64_t c = c0; c < c1; ++c) {
+            const int d = depth[c], q = plotter[c];
+            if (d < 0 || d > kMaxDepth || q == 0 || q < -8 || q > 8) {
+                ok[(size_t)p] = 0;
+                return;
+            }
+            lo = std::min(lo, d);
+            hi = std::max(hi, d);
+        }
+        pmin[(size_t)p] = lo;
+        pmax[(size_t)p] = hi;
+    });
+    auto all_ok = [&](int parts) {
+        bool r = true;
+        for (int p = 0; p < parts; ++p) r = r && ok[(size_t)p];
+        return r;
+    };
+    auto serial = [&]() {
+        return ingest_serial(m, n_cells, depth, plotter, n_edges, edge_cells, edge_local, n_bnd, bnd_cell, bnd_local);
+    };
+    if (!all_ok(PC)) return serial();
+    m.min_depth = *std::min_element(pmin.begin(), pmin.end());
+    m.max_depth = *std::max_element(pmax.begin(), pmax.end());
+    // slot[3 c + l - 1]: the last claim of cell c's local edge l (edge e, or n_edges + j for boundary edge j)
+    // (not initialised: every slot is written before it is read, or the check fails
+    // earlier; the claims are relaxed atomic stores, plain stores on x86 and Arm)
+    std::unique_ptr<uint32_t[]> slot(new uint32_t[(size_t)(3 * n_cells)]);
+    auto put = [&](int64_t i, uint32_t v) { __atomic_store_n(&slot[(size_t)i], v, __ATOMIC_RELAXED); };
+    m.ea.resize((size_t)n_edges);
+    m.eb.resize((size_t)n_edges);
+    m.la.resize((size_t)n_edges);
+    m.lb.resize((size_t)n_edges);
+    m.bc.resize((size_t)n_bnd);
+    m.bl.resize((size_t)n_bnd);
+    parallel_parts(n_edges, PE, [&](int64_t e0, int64_t e1, int p) {
+        for (int64_t e = e0; e < e1; ++e) {
+            int64_t a = edge_cells[2 * e], b = edge_cells[2 * e + 1];
+            int la = edge_local[2 * e], lb = edge_local[2 * e + 1];
+            if (a < 0 || a >= n_cells || b < 0 || b >= n_cells || a == b || la < 1 || la > 3 || lb < 1 || lb > 3) {
+                ok[(size_t)p] = 0;
+                return;
+            }
+            put(3 * a + la - 1, (uint32_t)e);
+            put(3 * b + lb - 1, (uint32_t)e);
+            if (b < a) {
+                std::swap(a, b);
+                std::swap(la, lb);
+            }
+            m.ea[(size_t)e] = a;
+            m.eb[(size_t)e] = b;
+            m.la[(size_t)e] = (int8_t)la;
+            m.lb[(size_t)e] = (int8_t)lb;
+        }
+    });
+    if (!all_ok(PE)) return serial();
+    parallel_parts(n_bnd, PB, [&](int64_t j0, int64_t j1, int p) {
+        for (int64_t j = j0; j < j1; ++j) {
+            const int64_t c = bnd_cell[j];
+            const int l = bnd_local[j];
+            if (c < 0 || c >= n_cells || l < 1 || l > 3) {
+                ok[(size_t)p] = 0;
+                return;
+            }
+            put(3 * c + l - 1, (uint32_t)(n_edges + j));
+            m.bc[(size_t)j] = c;
+            m.bl[(size_t)j] = (int8_t)l;
+        }
+    });
+    if (!all_ok(PB)) return serial();
+    parallel_parts(n_edges, PE, [&](int64_t e0, int64_t e1, int p) {
+        for (int64_t e = e0; e < e1; ++e)
+            if (slot[(size_t)(3 * m.ea[(size_t)e] + m.la[(size_t)e] - 1)] != (uint32_t)e ||
+                slot[(size_t)(3 * m.eb[(size_t)e] + m.lb[(size_t)e] - 1)] != (uint32_t)e) {
+                ok[(size_t)p] = 0;
+                return;
+            }
+    });
+    if (!all_ok(PE)) return serial();
+    parallel_parts(n_bnd, PB, [&](int64_t j0, int64_t j1, int p) {
+        for (int64_t j = j0; j < j1; ++j)
+            if (slot[(size_t)(3 * m.bc[(size_t)j] + m.bl[(size_t)j] - 1)] != (uint32_t)(n_edges + j)) {
+                ok[(size_t)p] = 0;
+                return;
+            }
+    });
+    if (!all_ok(PB)) return serial();
     return SWE_OK;
 }
 

@@ -457,7 +457,7 @@ static std::vector<int32_t> spread_order(const std::vector<SegInfo>& seg_info) {
 int rebuild_tasks(swe_ctx* c) {
     std::vector<int64_t> seg_ptr;
     std::vector<SegInfo> seg_info;
-    std::vector<Task> tasks, xtasks;
+    hvec<Task> tasks, xtasks;
     for (int i = 0; i < n_inst(c); ++i) {
         int rc = build_tasks(c->mesh[(size_t)i], c->offset[(size_t)i], i, c->seg_cells, seg_ptr, seg_info, tasks,
                              xtasks);

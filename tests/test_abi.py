@@ -65,8 +65,11 @@ def _validate(m, **over):
                                          P(el), len(bc), P(bc), P(bl))
 
 
-def test_mesh_validation_rejects_corrupt_streams(swe_lib):
-    m = swe.uniform_mesh(5)
+@pytest.mark.parametrize("depth", [5, 18])
+def test_mesh_validation_rejects_corrupt_streams(swe_lib, depth):
+    """Corrupt streams are rejected with the first bad item named; at depth 18
+    (2^19 cells) the check runs in parts on host threads."""
+    m = swe.uniform_mesh(depth)
     assert _validate(m) == 0
     bad = m.edge_cells.copy()
     bad[3, 1] = m.n_cells + 5
@@ -83,6 +86,14 @@ def test_mesh_validation_rejects_corrupt_streams(swe_lib):
     dupc = m.edge_cells.copy()
     dupc[0] = dupc[1]
     assert _validate(m, edge_local=dup, edge_cells=dupc) == -1
+    assert "used twice" in _lib.last_error()
+    k = len(m.edge_cells) - 2  # a duplicate claim at the far end of the list (another part)
+    dup = m.edge_local.copy()
+    dup[k] = dup[3]
+    dupc = m.edge_cells.copy()
+    dupc[k] = dupc[3]
+    assert _validate(m, edge_local=dup, edge_cells=dupc) == -1
+    assert _lib.last_error() == "edge %d: a cell's local edge is used twice" % k
     p = m.plotter.copy()
     p[7] = 0
     assert _validate(m, plotter=p) == -1
