@@ -108,12 +108,12 @@ int set_error(int code, const char* fmt, ...);
 
 // Host passes over large meshes run on several threads: [0, n) is split into
 // `parts` contiguous ranges, fn(begin, end, part) runs each (part 0 on the
-// calling thread). Meshes below 2^18 items stay on one thread.
+// calling thread). Meshes below 2^20 items stay on one thread.
 #ifndef SWE_HOST_THREADS
 #define SWE_HOST_THREADS 16
 #endif
 inline int host_parts(int64_t n) {
-    if (n < ((int64_t)1 << 18)) return 1;
+    if (n < ((int64_t)1 << 20)) return 1;
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
     return (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)std::min(hw, SWE_HOST_THREADS), n >> 16}));
 }

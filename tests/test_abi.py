@@ -65,10 +65,10 @@ def _validate(m, **over):
                                          P(el), len(bc), P(bc), P(bl))
 
 
-@pytest.mark.parametrize("depth", [5, 18])
+@pytest.mark.parametrize("depth", [5, 20])
 def test_mesh_validation_rejects_corrupt_streams(swe_lib, depth):
-    """Corrupt streams are rejected with the first bad item named; at depth 18
-    (2^19 cells) the check runs in parts on host threads."""
+    """Corrupt streams are rejected with the first bad item named; at depth 20
+    (2^21 cells) the check runs in parts on host threads."""
     m = swe.uniform_mesh(depth)
     assert _validate(m) == 0
     bad = m.edge_cells.copy()
