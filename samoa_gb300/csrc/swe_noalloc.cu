@@ -12,10 +12,14 @@
 // scratch array is held by every GPU that loads the library until exit.
 //
 // The step itself is the same arithmetic as the fused kernel, in two passes:
-// one thread per edge writes the left/right updates into the scratch slots,
-// then one thread per cell sums its slots in local edge order, updates the
-// cell and reduces the CFL time step; the last block writes dt_new and the
-// refinement count and clears the accumulators for the next call.
+// one thread per edge writes the left/right updates into the scratch slots and
+// counts its claim on each slot, then one thread per cell checks that each of
+// its three slots was claimed exactly once, sums them in local edge order,
+// updates the cell and reduces the CFL time step; the last block writes dt_new
+// and the refinement count and clears the accumulators for the next call. A
+// slot claimed by no edge or by two edges makes the call report -1 refinements
+// instead of reading what an earlier call left in that slot.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -31,11 +35,13 @@ namespace swe_noalloc {
 using namespace swe;
 
 constexpr int64_t kNoAllocMaxCells = (int64_t)1 << 16;  // 65,536 cells
-constexpr size_t kAccBytes = 256;                        // accumulators, then the slots
-constexpr size_t kScratchBytes = kAccBytes + (size_t)12 * sizeof(double) * kNoAllocMaxCells;
+constexpr size_t kAccBytes = 256;                        // accumulators
+constexpr size_t kClaimBytes = (size_t)3 * sizeof(unsigned int) * kNoAllocMaxCells;
+constexpr size_t kScratchBytes = kAccBytes + kClaimBytes + (size_t)12 * sizeof(double) * kNoAllocMaxCells;
 
 // The scratch: [0, 256) accumulators {dt bits, refinements, finished blocks,
-// error}, then the edge-update slots [4 quantities][3 local edges][max cells].
+// error}, then the claim counts [3 local edges][max cells] (zero between
+// calls), then the edge-update slots [4 quantities][3 local edges][max cells].
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 __constant__ double k_leg[kMaxDepth + 2];
@@ -74,7 +80,8 @@ __device__ __forceinline__ State load(const Args& A, int64_t c) { return State{A
 template <int SOLVER>
 __global__ void edges_kernel(Args A, unsigned char* scratch) {
     Acc* acc = reinterpret_cast<Acc*>(scratch);
-    double* slots = reinterpret_cast<double*>(scratch + kAccBytes);
+    unsigned int* claims = reinterpret_cast<unsigned int*>(scratch + kAccBytes);
+    double* slots = reinterpret_cast<double*>(scratch + kAccBytes + kClaimBytes);
     const int64_t M = kNoAllocMaxCells;
     const int64_t total = A.n_edges + A.n_bnd;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -107,6 +114,8 @@ __global__ void edges_kernel(Args A, unsigned char* scratch) {
             atomicOr(&acc->error, 1u);
             continue;
         }
+        atomicAdd(&claims[iL * M + L], 1u);
+        if (R >= 0) atomicAdd(&claims[iR * M + R], 1u);
         const double n1 = k_normal[pL][iL][0], n2 = k_normal[pL][iL][1];
         const State QL = load(A, L);
         State QR;
@@ -137,7 +146,8 @@ __global__ void edges_kernel(Args A, unsigned char* scratch) {
 
 __global__ void cells_kernel(Args A, unsigned char* scratch) {
     Acc* acc = reinterpret_cast<Acc*>(scratch);
-    const double* slots = reinterpret_cast<const double*>(scratch + kAccBytes);
+    unsigned int* claims = reinterpret_cast<unsigned int*>(scratch + kAccBytes);
+    const double* slots = reinterpret_cast<const double*>(scratch + kAccBytes + kClaimBytes);
     const int64_t M = kNoAllocMaxCells;
     __shared__ double red_min[32];
     __shared__ long long red_sum[32];
@@ -146,8 +156,16 @@ __global__ void cells_kernel(Args A, unsigned char* scratch) {
     double dtmin = DBL_MAX;
     long long nref = 0;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < A.n_cells; c += (int64_t)gridDim.x * blockDim.x) {
+        // each slot must hold exactly one edge's update of this call; the
+        // counts go back to zero for the next call whatever they were
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            bad |= claims[k * M + c] != 1u;
+            claims[k * M + c] = 0u;
+        }
         const int d = A.depth[c];
-        if (d < 0 || d > kMaxDepth) {
+        if (bad || d < 0 || d > kMaxDepth) {
             atomicOr(&acc->error, 1u);
             continue;
         }
@@ -232,39 +250,94 @@ __global__ void cells_kernel(Args A, unsigned char* scratch) {
     }
 }
 
-// Once per device, with that device current: the scratch array's device
-// address and the geometry tables of this file's kernels.
+// Once per device and CUDA context, with that device current: the scratch
+// array's device address, the geometry tables of this file's kernels, and the
+// accumulators and claim counts cleared. The context is recognised by its
+// unique id (cuCtxGetId, reached through the runtime's driver entry point, so
+// the library needs no link to the driver library): a device reset followed by
+// a new primary context gets a new id and so a fresh set-up, instead of running
+// on zeroed tables.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
 struct DeviceSetup {
     bool ready = false;
+    unsigned long long ctx_id = 0;
     unsigned char* scratch = nullptr;
 };
 static std::mutex g_setup_mutex;
 static DeviceSetup g_setup[64];
+static CtxGetCurrentFn g_ctx_current = nullptr;
+static CtxGetIdFn g_ctx_id = nullptr;
+
+static int driver_entry_points() {
+    if (g_ctx_current && g_ctx_id) return SWE_OK;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+        return set_error(SWE_E_CUDA, "swe_step_noalloc: driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
+    g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+    return SWE_OK;
+}
+
+// The current context's id, 0 when the calling thread has none yet.
+static unsigned long long current_ctx_id() {
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (g_ctx_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 static int setup_device(int dev, unsigned char** scratch) {
     if (dev < 0 || dev >= 64) return set_error(SWE_E_INVALID, "device %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_setup_mutex);
+    int rc = driver_entry_points();
+    if (rc) return rc;
     DeviceSetup& s = g_setup[dev];
-    if (!s.ready) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess)
-            return set_error(SWE_E_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
-        double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
-        geometry_tables(leg, vol, nrm);
-        e = cudaMemcpyToSymbol(k_leg, leg, sizeof(leg));
-        if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_vol, vol, sizeof(vol));
-        if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_normal, nrm, sizeof(nrm));
-        if (e != cudaSuccess) return set_error(SWE_E_CUDA, "geometry tables: %s", cudaGetErrorString(e));
-        // clear the accumulators (each call's last block clears them again)
-        e = cudaMemset(p, 0, kAccBytes);
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
-        if (e != cudaSuccess) return set_error(SWE_E_CUDA, "scratch init: %s", cudaGetErrorString(e));
-        s.scratch = static_cast<unsigned char*>(p);
-        s.ready = true;
+    unsigned long long id = current_ctx_id();
+    if (s.ready && id != 0 && id == s.ctx_id) {
+        *scratch = s.scratch;
+        return SWE_OK;
     }
+    // binds the device's primary context to this thread if it is not yet
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess)
+        return set_error(SWE_E_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+    id = current_ctx_id();
+    if (id == 0) return set_error(SWE_E_CUDA, "swe_step_noalloc: no current CUDA context on device %d", dev);
+    if (s.ready && id == s.ctx_id) {  // same context, first call from this thread
+        *scratch = s.scratch;
+        return SWE_OK;
+    }
+    s.ready = false;
+    double leg[kMaxDepth + 2], vol[kMaxDepth + 1], nrm[17][3][2];
+    geometry_tables(leg, vol, nrm);
+    e = cudaMemcpyToSymbol(k_leg, leg, sizeof(leg));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_vol, vol, sizeof(vol));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(k_normal, nrm, sizeof(nrm));
+    if (e != cudaSuccess) return set_error(SWE_E_CUDA, "geometry tables: %s", cudaGetErrorString(e));
+    // accumulators and claim counts start at zero (each call clears them again)
+    e = cudaMemset(p, 0, kAccBytes + kClaimBytes);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return set_error(SWE_E_CUDA, "scratch init: %s", cudaGetErrorString(e));
+    s.scratch = static_cast<unsigned char*>(p);
+    s.ctx_id = id;
+    s.ready = true;
     *scratch = s.scratch;
     return SWE_OK;
+}
+
+// After a launch failed part-way, the accumulators and claim counts may hold
+// this call's partial work: clear them on the stream so the next call starts
+// from zero (a memset, no allocation).
+static void clear_after_failure(unsigned char* scratch, cudaStream_t s) {
+    (void)cudaMemsetAsync(scratch, 0, kAccBytes + kClaimBytes, s);
 }
 
 }  // namespace swe_noalloc
@@ -281,7 +354,9 @@ extern "C" int swe_step_noalloc(const swe_params* p, int64_t n_cells, const int8
     if (n_cells < 1 || n_cells > kNoAllocMaxCells)
         return set_error(SWE_E_INVALID, "swe_step_noalloc: n_cells %lld outside 1..%lld (the fixed scratch limit)",
                          (long long)n_cells, (long long)kNoAllocMaxCells);
-    if (n_edges < 0 || n_bnd < 0 || 2 * n_edges + n_bnd != 3 * n_cells)
+    // both counts are bounded before they enter the sum, which then cannot overflow
+    if (n_edges < 0 || n_bnd < 0 || n_edges > 3 * kNoAllocMaxCells || n_bnd > 3 * kNoAllocMaxCells ||
+        2 * n_edges + n_bnd != 3 * n_cells)
         return set_error(SWE_E_INVALID, "swe_step_noalloc: edge counts inconsistent");
     if (!depth || !plotter || (n_edges && (!edge_cells || !edge_local)) || (n_bnd && (!bnd_cell || !bnd_local)) ||
         !h || !hu || !hv || !b || !h_out || !hu_out || !hv_out)
@@ -324,9 +399,15 @@ extern "C" int swe_step_noalloc(const swe_params* p, int64_t n_cells, const int8
         default: return set_error(SWE_E_INVALID, "swe_step_noalloc: unknown solver %d", p->solver);
     }
     e = cudaGetLastError();
-    if (e != cudaSuccess) return set_error(SWE_E_CUDA, "edges kernel: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        clear_after_failure(scratch, s);
+        return set_error(SWE_E_CUDA, "edges kernel: %s", cudaGetErrorString(e));
+    }
     cells_kernel<<<cblocks, threads, 0, s>>>(A, scratch);
     e = cudaGetLastError();
-    if (e != cudaSuccess) return set_error(SWE_E_CUDA, "cells kernel: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        clear_after_failure(scratch, s);
+        return set_error(SWE_E_CUDA, "cells kernel: %s", cudaGetErrorString(e));
+    }
     return SWE_OK;
 }
