@@ -386,6 +386,19 @@ int swe_division_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t*
  * No counterpart in the reference. */
 int swe_multiply_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t* mismatches);
 
+/* Test-only device fault injection, off by default. No counterpart in the
+ * reference (it has no bounded waits: it asserts). SWE_INJECT_STAGING_TX: the
+ * step kernel arms each staging mbarrier for 16 bytes more than its bulk copies
+ * deliver, so the phase never completes; every copy still lands, and the
+ * kernel's bounded wait (shortened to 20 ms) gives up, the CTA leaves its
+ * segment and the step reports SWE_E_DEVICE at the next swe_synchronize. The
+ * report clears the device flag; the failed step's state is undefined, so
+ * upload a state (or a mesh) before stepping on. Applies to device-resident
+ * steps (swe_traverse); stays set until SWE_INJECT_NONE. */
+#define SWE_INJECT_NONE 0
+#define SWE_INJECT_STAGING_TX 1
+int swe_set_fault_injection(swe_ctx* ctx, int32_t kind);
+
 /* One time step on caller-owned device memory, allocating nothing. No
  * counterpart in the reference. For callers that cannot allocate device memory
  * at the point where they step (a host code whose device memory all comes from
@@ -396,16 +409,21 @@ int swe_multiply_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t*
  * uses dt as given (no clamps), the traversal parity `parity` (0 = the given
  * cell order, 1 = reversed, as on the odd steps after an upload), and writes
  * min(volume / sum(len * speed)) to *dt_new and the refinement count to
- * *n_refinements (-1 if an index was out of range), both device pointers.
+ * *n_refinements, both device pointers. *n_refinements is -1 (and the outputs
+ * undefined) when the mesh is invalid: an index or a local edge number out of
+ * range, a plotter type or depth out of range, or a (cell, local edge) slot that
+ * no edge or more than one edge claims; the next call starts clean.
  * The work goes on `stream` (a cudaStream_t; NULL = the legacy default stream)
  * and the call returns without synchronising.
- * Limits: n_cells <= 65,536. The scratch (edge updates and reduction
- * accumulators, 6.3 MB) is one fixed array in device memory that every GPU which
- * loads the library keeps until exit; all calls share it, so calls that overlap
- * on the GPU (different streams, or without ordering) race. The first call on a
- * device sets it up (cudaGetSymbolAddress, geometry tables, clearing the
- * accumulators, one device synchronisation): make that first call before any
- * stream capture. */
+ * Limits: n_cells <= 65,536. The scratch (edge updates, per-slot claim counts
+ * and reduction accumulators, 7.1 MB) is one fixed array in device memory that
+ * every GPU which loads the library keeps until exit; all calls share it, so
+ * calls that overlap on the GPU (different streams, or without ordering) race.
+ * The first call on a
+ * device, and the first after that device's context was replaced (a device
+ * reset), sets it up (cudaGetSymbolAddress, geometry tables, clearing the
+ * accumulators and claim counts, one device synchronisation): make that first
+ * call before any stream capture. */
 int swe_step_noalloc(const swe_params* params, int64_t n_cells, const int8_t* depth, const int8_t* plotter,
                      int64_t n_edges, const int64_t* edge_cells, const int8_t* edge_local, int64_t n_bnd,
                      const int64_t* bnd_cell, const int8_t* bnd_local, const double* h, const double* hu,

@@ -25,7 +25,7 @@ EXPORTS = [
     "swe_division_check", "swe_step_host", "swe_gauge_gradient",
     "swe_traverse_gauges", "swe_mesh_uniform_vertices", "swe_mesh_build", "swe_mesh_adapt",
     "swe_multiply_check", "swe_set_staging", "swe_get_task_counts", "swe_set_cross_pass", "swe_traverse_frozen",
-    "swe_set_segment_order",
+    "swe_set_segment_order", "swe_set_fault_injection",
 ]
 
 
@@ -86,6 +86,7 @@ def load():
         "swe_ensemble_get_refinements": [P, P, P],
         "swe_traverse_graph": [P, i64],
         "swe_set_dt_sequence": [P, i64, P],
+        "swe_set_fault_injection": [P, i32],
         "swe_step_noalloc": [P, i64, P, P, i64, P, P, i64, P, P, P, P, P, P, P, P, P, P, dbl, i32, P, P, P],
         "swe_snapshot_store": [P, P, P, P, P],
         "swe_snapshot_restore": [P, P, P, P, i64],

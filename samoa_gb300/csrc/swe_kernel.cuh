@@ -72,6 +72,8 @@ struct StepArgs {
     int32_t fixed_io;          // 1: read h[0], hu[0], hv[0] and write h[1].. on every step (caller's buffers)
     int32_t stage_depth;       // 1: stage a segment, then work on it; 2: stage the next one meanwhile
     int32_t halo_solve;        // 1: solve the halo tasks here (no cross-edge pass); 0: copy the pass's updates
+    uint32_t extra_tx;         // fault injection only: bytes the staging barrier expects beyond the copies (0)
+    unsigned long long wait_ns;  // limit of one mbarrier wait, in ns of the global timer
 };
 
 // Launch bounds of the step kernel: at most 256 threads; with SWE_MIN_BLOCKS
@@ -83,7 +85,17 @@ struct StepArgs {
 #define SWE_STEP_BOUNDS __launch_bounds__(256)
 #endif
 
-constexpr int kWaitLimit = 1 << 24;  // polls of an mbarrier before a kernel gives up
+// An mbarrier wait gives up after wait_ns of the global timer (1 s by default;
+// the copies it waits for take microseconds), or after kPollLimit polls
+// whatever the timer says, so that every wait ends.
+constexpr unsigned long long kWaitNs = 1000000000ull;
+constexpr unsigned int kPollLimit = 1u << 30;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -299,7 +311,7 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             if (tid == 0) {
                 fence_proxy_async();
                 const uint32_t bytes = (uint32_t)cbulk * 8u;
-                mbar_arrive_expect_tx(&bar[k], 4u * bytes);
+                mbar_arrive_expect_tx(&bar[k], 4u * bytes + A.extra_tx);
                 bulk_g2s(bh, hin + c0, bytes, &bar[k]);
                 bulk_g2s(bh + T, huin + c0, bytes, &bar[k]);
                 bulk_g2s(bh + 2 * T, hvin + c0, bytes, &bar[k]);
@@ -318,9 +330,16 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     auto wait = [&](int k) {
         if (pending & (1u << k)) {
             if (tid == 0) {
-                int polls = 0;
+                unsigned int polls = 0;
+                unsigned long long t0 = 0;
                 while (!mbar_try_wait(&bar[k], (phase >> k) & 1u)) {
-                    if (++polls > kWaitLimit) {
+                    ++polls;
+                    if ((polls & 63u) == 1u) {
+                        const unsigned long long now = global_ns();
+                        if (polls == 1u) t0 = now;
+                        else if (now - t0 > A.wait_ns) polls = kPollLimit;
+                    }
+                    if (polls >= kPollLimit) {
                         s_error = 2u;
                         break;
                     }

@@ -256,6 +256,7 @@ struct swe_ctx {
     int32_t arith = SWE_ARITH_STRICT;
     int32_t cross_mode = SWE_CROSS_AUTO;
     int32_t seg_order_mode = SWE_ORDER_AUTO;
+    int32_t inject = SWE_INJECT_NONE;               // test-only device fault injection
     int64_t n_seg = 0, n_tasks = 0;
     int grid = 0, max_ndepth = 1;
     size_t smem = 0;
@@ -522,9 +523,14 @@ int check_device_error(swe_ctx* c) {
     unsigned int err = 0;
     CUDA_TRY(cudaMemcpyAsync(&err, &c->gs->error, sizeof(err), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
-    if (err)
+    if (err) {
+        // reported once: the flag is cleared so that the context steps on after
+        // the caller has uploaded a state again (the failed step's is undefined)
+        CUDA_TRY(cudaMemsetAsync(&c->gs->error, 0, sizeof(err), c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
         return set_error(SWE_E_DEVICE, "step kernel reported error 0x%x (%s)", err,
                          (err & 2u) ? "TMA wait ran out" : "edge task index out of range");
+    }
     return SWE_OK;
 }
 
@@ -681,6 +687,11 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     A.use_tma = use_tma;
     A.stage_depth = c->stage_depth;
     A.fixed_io = 0;
+    // fault injection (tests): the staging barrier expects 16 bytes that no copy
+    // delivers, so its phase never completes and the bounded wait, shortened to
+    // 20 ms, gives up; every issued copy still lands before the CTA leaves
+    A.extra_tx = c->inject == SWE_INJECT_STAGING_TX ? 16u : 0u;
+    A.wait_ns = c->inject == SWE_INJECT_STAGING_TX ? 20000000ull : kWaitNs;
     // edges between two segments: a pass before the step kernel for device-resident
     // steps; solved by both segments' CTAs when the state is in host memory (the
     // pass's scattered reads of host memory cost more than the duplicated solves)
@@ -1392,6 +1403,14 @@ int swe_get_step_count(swe_ctx* c, int64_t* steps) {
     CUDA_TRY(cudaMemcpyAsync(&s, &c->gs->step, sizeof(s), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     *steps = s;
+    return SWE_OK;
+}
+
+int swe_set_fault_injection(swe_ctx* c, int32_t kind) {
+    if (!c) return set_error(SWE_E_INVALID, "null context");
+    if (kind != SWE_INJECT_NONE && kind != SWE_INJECT_STAGING_TX)
+        return set_error(SWE_E_INVALID, "unknown fault injection %d", kind);
+    c->inject = kind;
     return SWE_OK;
 }
 
