@@ -1,6 +1,7 @@
 """Build recipe for the oracle (test infrastructure only).
 
-Compiles ``swe_oracle.c`` into ``oracle/_build/libswe_oracle.so`` with strict IEEE
+Compiles ``swe_oracle.c`` (the step) and ``swe_oracle_adapt.c`` (one adaption
+step and the integrated bathymetry) into ``oracle/_build/libswe_oracle.so`` with strict IEEE
 flags: no FMA contraction, no fast-math, OpenMP for the timed CPU baseline.
 The reference itself is Fortran and is not compiled here (no Fortran compiler).
 """
@@ -10,7 +11,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libswe_oracle.so")
-SRC = os.path.join(HERE, "swe_oracle.c")
+SRCS = [os.path.join(HERE, "swe_oracle.c"), os.path.join(HERE, "swe_oracle_adapt.c")]
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-fno-fast-math", "-ffp-contract=off",
           "-fno-strict-aliasing", "-fopenmp", "-Wall", "-Wno-unused-function"]
@@ -18,10 +19,10 @@ CFLAGS = ["-O2", "-fPIC", "-shared", "-std=c11", "-fno-fast-math", "-ffp-contrac
 
 def build(force: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in SRCS):
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", *CFLAGS, SRC, "-o", tmp, "-lm"])
+    subprocess.check_call(["gcc", *CFLAGS, *SRCS, "-o", tmp, "-lm"])
     os.replace(tmp, LIB)
     return LIB
 

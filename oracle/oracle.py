@@ -2,7 +2,8 @@
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
 may import this module, and only as the checker. It wraps ``swe_oracle.c``, the
-strict-IEEE C restatement of sam(oa)^2's SWE Euler step.
+strict-IEEE C restatement of sam(oa)^2's SWE Euler step, and ``swe_oracle_adapt.c``,
+the restatement of one adaption step and of the integrated bathymetry.
 """
 import ctypes as C
 import os
@@ -55,6 +56,10 @@ def lib():
         L.oracle_cell_slots.restype = i32
         L.oracle_cell_slots.argtypes = [i64, i64, P, P, i64, P, P, P]
         L.oracle_max_threads.restype = i32
+        L.oracle_bathymetry_cells.restype = i32
+        L.oracle_bathymetry_cells.argtypes = [i64, P, P, P]
+        L.oracle_adapt.restype = i64
+        L.oracle_adapt.argtypes = [i64, P, P, P, P, P, P, P, i64, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -238,3 +243,44 @@ class OmpState:
 
 def max_threads():
     return lib().oracle_max_threads()
+
+
+BATHYMETRY_KINDS = {"flat": 0, "bowl": 1}
+
+
+def bath_spec(kind, p0, p1=0.0, scaling=1.0, offset=(0.0, 0.0), max_depth=0):
+    """The bathymetry the oracle samples: "flat" (constant p0) or "bowl"
+    (-p0 * (1 - r^2 / p1^2)), world coordinates scaling * x + offset, integrated
+    over 2^min(16, max_depth - depth) sub-triangles of a cell."""
+    return np.array([BATHYMETRY_KINDS[kind], p0, p1, scaling, offset[0], offset[1], max_depth], np.float64)
+
+
+def bathymetry_cells(depths, spec):
+    """get_bathymetry_at_element of every leaf of the tree with these depths."""
+    d = np.ascontiguousarray(depths, np.int8)
+    out = np.empty(len(d), np.float64)
+    rc = lib().oracle_bathymetry_cells(len(d), _p(d), _p(np.ascontiguousarray(spec, np.float64)), _p(out))
+    if rc != 0:
+        raise RuntimeError("oracle_bathymetry_cells failed: %d" % rc)
+    return out
+
+
+def adapt(depths, flags, h=None, hu=None, hv=None, b=None, spec=None):
+    """One adaption step (conformity, refine/coarsen, order-0 transfer; refined
+    cells' b integrated from `spec` when given, else copied). Returns
+    (depth, source, [h, hu, hv, b]) with None for the state not given."""
+    d = np.ascontiguousarray(depths, np.int8)
+    f = np.ascontiguousarray(flags, np.int8)
+    n = len(d)
+    ins = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (h, hu, hv, b)]
+    cap = 4 * n
+    dout = np.empty(cap, np.int8)
+    src = np.empty(cap, np.int64)
+    outs = [None if a is None else np.empty(cap, np.float64) for a in ins]
+    q = lambda a: None if a is None else _p(a)
+    sp = None if spec is None else np.ascontiguousarray(spec, np.float64)
+    m = lib().oracle_adapt(n, _p(d), _p(f), *[q(a) for a in ins], q(sp), cap, _p(dout), _p(src),
+                           *[q(a) for a in outs])
+    if m < 0:
+        raise RuntimeError("oracle_adapt failed: %d" % m)
+    return dout[:m].copy(), src[:m].copy(), [None if a is None else a[:m].copy() for a in outs]

@@ -27,6 +27,52 @@ def _world(mesh, cfg):
     return cfg.scaling * c[:, 0] + cfg.offset[0], cfg.scaling * c[:, 1] + cfg.offset[1]
 
 
+def element_bathymetry(vertices, depth, max_depth, bathymetry, scaling, offset, chunk=1 << 20):
+    """b of each cell as get_bathymetry_at_element computes it with _ADAPT_INTEGRATE
+    (src/SWE/SWE_initialize.f90:105-147): the mean of ``bathymetry(x, y)`` over
+    2^min(16, max_depth - depth) sub-triangles of the cell, each sampled at its
+    centroid (x1 + x2 + x3) / 3 in world coordinates scaling * x + offset. The
+    sub-triangles come from bisecting the hypotenuse: (x1, x2, x3), x2 the right
+    angle, splits into (x1, m, x2) and (x2, m, x3), m = (x1 + x3) / 2; the mean is
+    taken pairwise up the bisection tree, 0.5 * (first + second), as the
+    reference's recursion does, so the rounding is the same. ``vertices`` is
+    [n, 3, 2] in the unit square (the mesh builder's, right angle in the middle)."""
+    vertices = np.asarray(vertices, np.float64)
+    depth = np.asarray(depth)
+    n = len(depth)
+    out = np.empty(n, np.float64)
+    dd = np.clip(max_depth - depth.astype(np.int64), 0, 16)
+    for k in np.unique(dd):
+        idx = np.nonzero(dd == k)[0]
+        step = max(1, chunk >> int(k))
+        for s in range(0, len(idx), step):
+            sel = idx[s:s + step]
+            v3 = vertices[sel]
+            x1, x2, x3 = v3[:, None, 0], v3[:, None, 1], v3[:, None, 2]  # [m, 1, 2] each
+            for _ in range(int(k)):
+                mid = 0.5 * (x1 + x3)
+                shape = (len(sel), 2 * x1.shape[1], 2)
+                y1, y2, y3 = np.empty(shape), np.empty(shape), np.empty(shape)
+                y1[:, 0::2], y2[:, 0::2], y3[:, 0::2] = x1, mid, x2  # first child (x1, m, x2)
+                y1[:, 1::2], y2[:, 1::2], y3[:, 1::2] = x2, mid, x3  # second child (x2, m, x3)
+                x1, x2, x3 = y1, y2, y3
+            c = ((x1 + x2) + x3) / 3.0
+            v = bathymetry(scaling * c[:, :, 0] + offset[0], scaling * c[:, :, 1] + offset[1])
+            v = np.broadcast_to(np.asarray(v, np.float64), c.shape[:2])
+            for _ in range(int(k)):
+                v = 0.5 * (v[:, 0::2] + v[:, 1::2])
+            out[sel] = v[:, 0]
+    return out
+
+
+def _vertices(mesh):
+    """[n, 3, 2] vertices of a mesh's cells in the unit square (right angle in the middle)."""
+    if mesh.vertices is not None:
+        return mesh.vertices
+    from .swe import mesh_from_depths
+    return mesh_from_depths(mesh.depth, centroids=False, vertices=True).vertices
+
+
 def _grid(mesh, cfg, h, b):
     n = mesh.n_cells
     hu = np.zeros(n)
@@ -109,7 +155,9 @@ def parabolic_bowl(log2_cells=14, seed=2, solver="aug_riemann", amplitude=0.5, s
                    min_depth=None, max_depth=None):
     """Parabolic bowl b(r) = -10 (1 - r^2 / 0.4^2) on [-0.5, 0.5]^2 (dry land for
     r > 0.4) with a Gaussian surface bump at a seeded offset; dry tolerance 1e-3 m.
-    On a frozen uniform mesh (the remeshing of the adaptive case stays on the host)."""
+    On a frozen uniform mesh (the remeshing of the adaptive case stays on the host).
+    b is integrated over each cell as the initialisation does (element_bathymetry,
+    down to the maximum depth); the surface is sampled at the centroid."""
     d = log2_cells - 1
     cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=1e-3, scaling=1.0,
                  offset=(-0.5, -0.5), i_min_depth=d if min_depth is None else min_depth,
@@ -118,7 +166,7 @@ def parabolic_bowl(log2_cells=14, seed=2, solver="aug_riemann", amplitude=0.5, s
     x, y = _world(mesh, cfg)
     rng = np.random.default_rng(seed)
     x0, y0 = rng.uniform(-0.1, 0.1, 2)
-    b = bowl_bathymetry(x, y)
+    b = element_bathymetry(_vertices(mesh), mesh.depth, cfg.i_max_depth, bowl_bathymetry, cfg.scaling, cfg.offset)
     eta = amplitude * np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / (2 * sigma * sigma))
     # surface = eta over water; on land the state is dry: h = b (depth 0)
     h = np.where(b < eta, eta, b)
@@ -129,7 +177,9 @@ def adaptive_bowl(min_depth=12, max_depth=22, seed=2, solver="aug_riemann", ampl
     """The parabolic bowl on the mesh of the a-priori refinement between the given
     depths (the adaptive wet/dry configuration: the Gaussian surface differs
     between the vertices of every cell, so the initial mesh is uniform at the
-    maximum depth; the flags of the step then coarsen the flat water)."""
+    maximum depth; the flags of the step then coarsen the flat water). b is
+    integrated over each cell (element_bathymetry), as refined cells get it
+    during the run (run_adaptive with ``scn.bathymetry``)."""
     cfg = Config(flux_solver=solver, boundary="outflow", courant_number=0.45, dry_tolerance=1e-3, scaling=1.0,
                  offset=(-0.5, -0.5), i_min_depth=min_depth, i_max_depth=max_depth)
     rng = np.random.default_rng(seed)
@@ -137,7 +187,7 @@ def adaptive_bowl(min_depth=12, max_depth=22, seed=2, solver="aug_riemann", ampl
     eta_f = lambda x, y: amplitude * np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / (2 * sigma * sigma))
     mesh = apriori_mesh(cfg, eta_f)
     x, y = _world(mesh, cfg)
-    b = bowl_bathymetry(x, y)
+    b = element_bathymetry(mesh.vertices, mesh.depth, max_depth, bowl_bathymetry, cfg.scaling, cfg.offset)
     eta = eta_f(x, y)
     h = np.where(b < eta, eta, b)
     scn = Scenario("adaptive_bowl", _grid(mesh, cfg, h, b), cfg, 500)

@@ -420,12 +420,32 @@ def initial_dt(mesh: Mesh, h, hu, hv, b, courant):
     return courant * best
 
 
+def remesh(cfg, mesh, flags, h, hu, hv, b, bathymetry=None):
+    """One remesh of the run loop: the adaption step from the time step's flags
+    (swe_mesh_adapt: conformity, refine/coarsen, order-0 transfer), with refined
+    cells' b integrated from `bathymetry(x, y)` when it is given (refine_op's
+    get_bathymetry_at_element, src/SWE/SWE_adapt.f90:132, with _ADAPT_INTEGRATE),
+    else their parent's. Returns the new mesh and (h, hu, hv, b)."""
+    new, (h, hu, hv, b), src = adapt(mesh, flags, h, hu, hv, b, with_source=True)
+    if bathymetry is not None and b is not None:
+        from .scenarios import element_bathymetry
+        fine = new.depth > mesh.depth[src]
+        if fine.any():
+            ver = new.vertices
+            if ver is None:
+                ver = mesh_from_depths(new.depth, centroids=False, vertices=True).vertices
+            b[fine] = element_bathymetry(ver[fine], new.depth[fine], cfg.i_max_depth, bathymetry, cfg.scaling,
+                                         cfg.offset)
+    return new, (h, hu, hv, b)
+
+
 def run_adaptive(cfg, mesh, h, hu, hv, b, dt, steps, adapt_every=1, bathymetry=None, device=0, time=0.0):
     """The SWE run loop with host remeshing (src/SWE/SWE.f90:378-392): step i
     (from 1) is preceded by a remesh when i % adapt_every == 0, from the
     refinement flags of the step before (swe_mesh_adapt + swe_mesh_build, then
-    an upload); refined cells take b from `bathymetry(x, y)` when it is given
-    (get_bathymetry_at_element of refine_op), else their parent's. Returns the
+    an upload); refined cells take b integrated from `bathymetry(x, y)` when it
+    is given (get_bathymetry_at_element of refine_op, src/SWE/SWE_adapt.f90:132,
+    with _ADAPT_INTEGRATE: scenarios.element_bathymetry), else their parent's. Returns the
     final (mesh, h, hu, hv, b, time, dt) and timings: device seconds of the steps
     (CUDA events) and host seconds of the remeshes and uploads."""
     import time as _time
@@ -449,14 +469,7 @@ def run_adaptive(cfg, mesh, h, hu, hv, b, dt, steps, adapt_every=1, bathymetry=N
                 h, hu, hv, b = ctx.download_state()
                 time, dt, _ = ctx.get_time()
                 t1 = _time.perf_counter()
-                new, (h, hu, hv, b), src = adapt(mesh, flags, h, hu, hv, b, with_source=True)
-                if bathymetry is not None:
-                    fine = new.depth > mesh.depth[src]
-                    if fine.any():
-                        x = cfg.scaling * new.centroids[fine, 0] + cfg.offset[0]
-                        y = cfg.scaling * new.centroids[fine, 1] + cfg.offset[1]
-                        b[fine] = bathymetry(x, y)
-                mesh = new
+                mesh, (h, hu, hv, b) = remesh(cfg, mesh, flags, h, hu, hv, b, bathymetry)
                 t2 = _time.perf_counter()
                 ctx.upload_mesh(mesh)
                 ctx.upload_state(h, hu, hv, b)

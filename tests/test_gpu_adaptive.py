@@ -45,20 +45,31 @@ def test_adaptive_mesh_step_bitexact(swe_lib, oracle_lib, solver):
         ctx.close()
 
 
+def bowl_spec(cfg):
+    return O.bath_spec("bowl", 10.0, 0.4, cfg.scaling, cfg.offset, cfg.i_max_depth)
+
+
 def test_remesh_cycles_bitexact(swe_lib, oracle_lib):
-    """Five cycles of four steps, each followed by a host remesh from the last
-    step's flags; the oracle walks the same trees with the same transferred
-    states, and the GPU matches it bit for bit after every step."""
+    """Five cycles of four steps, each followed by a remesh from the last
+    step's flags: the product remeshes on the host (swe.remesh) and the GPU
+    steps on its trees; the oracle remeshes on its own (oracle_adapt, with the
+    integrated bathymetry for refined cells) and walks its own trees. Trees,
+    transferred states and b agree at every remesh, and the GPU matches the
+    oracle bit for bit after every step."""
     scn = scenarios.adaptive_bowl(min_depth=6, max_depth=11, solver="fwave")
     g = scn.grid
-    P = oracle_params(scn.cfg)
+    cfg = scn.cfg
+    P = oracle_params(cfg)
+    spec = bowl_spec(cfg)
     mesh, h, hu, hv, b, t, dt = g.mesh, g.h, g.hu, g.hv, g.b, g.r_time, g.r_dt
+    od, ost = mesh.depth.copy(), [h, hu, hv, O.bathymetry_cells(mesh.depth, spec)]
+    assert np.array_equal(ost[3], b)
     ctx = swe.SweContext(0)
     sizes = []
     try:
         for cycle in range(5):
-            o = O.mesh_from_depths(mesh.depth)
-            W = O.WalkState(o["cells5"], h, hu, hv, b, t, dt)
+            o = O.mesh_from_depths(od)
+            W = O.WalkState(o["cells5"], *ost, t, dt)
             _upload(ctx, scn, mesh, h, hu, hv, b, t, dt)
             for k in range(4):
                 W.steps(P, 1)
@@ -69,7 +80,11 @@ def test_remesh_cycles_bitexact(swe_lib, oracle_lib):
             assert np.array_equal(flags, W.flags)
             t, dt, _ = ctx.get_time()
             assert (t, dt) == (W.time, W.dt)
-            mesh, (h, hu, hv, b) = swe.adapt(mesh, flags, gh, ghu, ghv, b)
+            mesh, (h, hu, hv, b) = swe.remesh(cfg, mesh, flags, gh, ghu, ghv, b, scenarios.bowl_bathymetry)
+            od, _, ost = O.adapt(od, W.flags, W.h, W.hu, W.hv, W.b, spec=spec)
+            assert np.array_equal(mesh.depth, od), "cycle %d: trees differ" % cycle
+            for name, x, y in zip(("h", "hu", "hv", "b"), (h, hu, hv, b), ost):
+                assert np.array_equal(x, y), "cycle %d: transferred %s differs" % (cycle, name)
             sizes.append(mesh.n_cells)
     finally:
         ctx.close()
