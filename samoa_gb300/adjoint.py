@@ -519,22 +519,32 @@ class WindowedGaugeProblem:
         finally:
             P.close()
         self.stats["windows"] = len(wins)
-        return Jsum, gh, gb
+        # J of the forward run, summed as objective() sums it (window by window on
+        # the host); the sweep's own sum of the windows' J takes another order
+        self.stats["J_sweep"] = Jsum
+        return J, gh, gb
 
 
 class GaugeMisfit(torch.autograd.Function):
-    """J(h0, b) for a GaugeProblem, differentiable with respect to h0 and b."""
+    """J(h0, b) for a GaugeProblem (or a WindowedGaugeProblem), differentiable
+    with respect to h0 and b. forward is one forward run (problem.objective);
+    backward runs the checkpointed reverse sweep (problem.gradient) from the
+    saved inputs, so an evaluation that needs no gradient pays no sweep."""
 
     @staticmethod
     def forward(ctx, h0, b, problem):
-        J, gh, gb = problem.gradient(h0, b)
-        ctx.save_for_backward(gh, gb)
+        J = problem.objective(h0, b)
+        ctx.problem = problem
+        ctx.save_for_backward(h0, b)
         return torch.tensor(J, dtype=torch.float64, device=h0.device)
 
     @staticmethod
     def backward(ctx, gJ):
-        gh, gb = ctx.saved_tensors
-        return gJ * gh.to(gJ.device), gJ * gb.to(gJ.device), None
+        h0, b = ctx.saved_tensors
+        _, gh, gb = ctx.problem.gradient(h0, b)
+        gh = torch.as_tensor(gh, dtype=torch.float64).to(gJ.device)
+        gb = torch.as_tensor(gb, dtype=torch.float64).to(gJ.device)
+        return gJ * gh, gJ * gb, None
 
 
 def record_dts(mesh, params, h0, b, steps, device=0):

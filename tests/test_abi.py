@@ -149,13 +149,26 @@ def test_initial_dt_matches_formula():
 
 def test_bench_reference_arm_json(tmp_path):
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
-                          "--warmup", "1", "--cpu-sample-log2", "12"], capture_output=True, text=True, timeout=300,
+                          "--warmup", "1", "--log2-cells", "12"], capture_output=True, text=True, timeout=300,
                          cwd=ROOT)
     assert out.returncode == 0, out.stderr
     line = [l for l in out.stdout.splitlines() if l.startswith("{")][-1]
     j = json.loads(line)
     assert j["impl"] == "reference" and j["value"] > 0 and j["unit"] == "cell-updates/s"
     assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["cpu_baseline"]["kind"] == "port"
+    assert j["config"]["cells"] == 1 << 12  # the whole workload, not a sample
+
+
+def test_bench_reference_arm_loads_no_product_library():
+    """The CPU arm builds its workload on the oracle's own mesh: the GPU library
+    is never loaded, and the mesh equals the product's uniform mesh."""
+    code = ("import sys; sys.path.insert(0, %r); import bench, numpy as np; "
+            "s = bench.basin_from_oracle(10, 'fwave'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED' if 'libsamoa_swe' in maps else 'CLEAN', s.grid.mesh.n_cells)") % ROOT
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["CLEAN", "1024"]
 
 
 def test_bench_reference_arm_two_ranks_gloo():
@@ -164,7 +177,7 @@ def test_bench_reference_arm_two_ranks_gloo():
     out = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
                           "--master-addr", "127.0.0.1", "--master-port", "29517", os.path.join(ROOT, "bench.py"),
                           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1",
-                          "--cpu-sample-log2", "10"], capture_output=True, text=True, timeout=300, cwd=ROOT, env=env)
+                          "--log2-cells", "10"], capture_output=True, text=True, timeout=300, cwd=ROOT, env=env)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1

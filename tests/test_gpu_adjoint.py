@@ -184,17 +184,29 @@ def test_bathymetry_gradient_matches_branch_frozen_differences(swe_lib):
 
 
 def test_autograd_function(swe_lib):
+    """GaugeMisfit: forward is one forward run (T forward steps, no reverse
+    step), backward the checkpointed sweep; J and the gradients are those of
+    the problem's own objective and gradient."""
     import torch
     case = scenarios.adjoint_case(log2_cells=10, steps=30, n_gauges=8, seed=6)
     P = adjoint.GaugeProblem(case["mesh"], case["params"], case["gauges"], case["obs"], case["dts"], snapshots=4)
     try:
         h0 = torch.tensor(case["h0"], device="cuda", requires_grad=True)
         b = torch.tensor(case["b"], device="cuda", requires_grad=True)
+        P.stats = {"forward_steps": 0, "adjoint_steps": 0}
         J = adjoint.GaugeMisfit.apply(h0, b, P)
+        assert P.stats == {"forward_steps": 30, "adjoint_steps": 0}
+        assert float(J.detach()) == P.objective(case["h0"], case["b"])
+        P.stats = {"forward_steps": 0, "adjoint_steps": 0}
         J.backward()
+        assert P.stats["adjoint_steps"] == 30 and P.stats["forward_steps"] >= 30
         J2, gh, gb = P.gradient(case["h0"], case["b"])
-        assert float(J.detach()) == J2
+        assert abs(float(J.detach()) - J2) <= 1e-12 * abs(J2)
         assert torch.equal(h0.grad, gh) and torch.equal(b.grad, gb)
+        with torch.no_grad():  # no gradient asked for: one forward run only
+            P.stats = {"forward_steps": 0, "adjoint_steps": 0}
+            adjoint.GaugeMisfit.apply(h0, b, P)
+            assert P.stats == {"forward_steps": 30, "adjoint_steps": 0}
     finally:
         P.close()
 
@@ -349,6 +361,8 @@ def test_windowed_gradient_matches_frozen_differences(swe_lib):
     P = adjoint.WindowedGaugeProblem(g.mesh, cfg, pts, obs, dts, window=window, snapshots=3)
     J, gh, gb = P.gradient(g.h, g.b)
     assert len(set(P.stats["cells"])) > 1, P.stats["cells"]
+    assert P.objective(g.h, g.b) == J
+    assert abs(P.stats["J_sweep"] - J) <= 1e-12 * abs(J)
     assert P.objective_frozen(g.h, g.b, record=True) == J
     assert P.objective_frozen(g.h, g.b, record=False) == J
     rng = np.random.default_rng(31)
