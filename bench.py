@@ -13,7 +13,7 @@ N > 1 runs N independent replicas (one per GPU, launched by torchrun); the
 path does not shard across GPUs here ("replicas only"). ``--impl reference``
 times the CPU implementation of the step (the project's OpenMP restatement of
 the reference's FP64 step; the reference itself is Fortran and is not built)
-on the host cores, on a bounded sample of the workload.
+on all host cores, on the whole workload, K steps in one call.
 """
 import argparse
 import json
@@ -48,19 +48,20 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="skip the tiling autotuner (default tiling)")
     ap.add_argument("--no-adaptive", action="store_true")
     ap.add_argument("--adaptive-min-depth", type=int, default=12)
-    ap.add_argument("--adaptive-max-depth", type=int, default=18)
-    ap.add_argument("--adaptive-steps", type=int, default=20)
+    ap.add_argument("--adaptive-max-depth", type=int, default=22)
+    ap.add_argument("--adaptive-steps", type=int, default=500)
     ap.add_argument("--tune-log2-cells", type=int, default=22)
-    ap.add_argument("--cpu-sample-log2", type=int, default=22)
-    ap.add_argument("--cpu-steps", type=int, default=500,
-                    help="steps of the CPU baseline on its sample (500 x 2^22 cells: ~10 s on 16 Grace cores)")
+    ap.add_argument("--cpu-steps", type=int, default=20,
+                    help="steps of the CPU baseline on the workload (20 x 2^26 cells: ~10 s on 16 Grace cores)")
     ap.add_argument("--segment-cells", type=int, default=0)
     ap.add_argument("--block-threads", type=int, default=0)
     ap.add_argument("--arith", default="strict", choices=["strict", "fma"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ensemble-instances", type=int, default=512)
-    ap.add_argument("--ensemble-steps", type=int, default=10)
+    ap.add_argument("--ensemble-steps", type=int, default=1000)
+    ap.add_argument("--ensemble-bucket-steps", type=int, default=50,
+                    help="steps of the per-size breakdown (batched and looped per log2-size bucket)")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--adjoint-log2-cells", type=int, default=18)
     ap.add_argument("--adjoint-steps", type=int, default=2000)
@@ -68,6 +69,8 @@ def parse():
     ap.add_argument("--adjoint-fd-frozen", type=int, default=16,
                     help="directions of the branch-frozen finite-difference check of the adjoint")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-moving", action="store_true")
+    ap.add_argument("--moving-log2-cells", type=int, default=22)
     return ap.parse_args()
 
 
@@ -163,20 +166,22 @@ def host_cpu():
     return {"model": model, "logical_cores": os.cpu_count()}
 
 
-def cpu_baseline(log2, steps, solver, threads):
-    """Time the OpenMP CPU step (the oracle's restatement of the reference step)
-    on a 2^log2-cell sample of the same basin workload."""
+def oracle_params_for(cfg):
     from oracle import oracle as O
-    from samoa_gb300 import scenarios, swe
-    scn = scenarios.ocean_basin(log2_cells=log2, solver=solver)
-    g = scn.grid
-    m = g.mesh
-    S = O.OmpState(m.depth, m.plotter, m.edge_cells, m.edge_local, m.bnd_cell, m.bnd_local, g.h, g.hu, g.hv, g.b,
-                   g.r_time, g.r_dt)
-    cfg = scn.cfg
-    P = O.make_params(solver=swe.SOLVERS[cfg.flux_solver], bc=swe.BOUNDARIES[cfg.boundary],
-                      dry_tolerance=cfg.dry_tolerance, courant=cfg.courant_number, scaling=cfg.scaling,
-                      min_depth=cfg.i_min_depth, max_depth=cfg.i_max_depth)
+    from samoa_gb300 import swe
+    return O.make_params(solver=swe.SOLVERS[cfg.flux_solver], bc=swe.BOUNDARIES[cfg.boundary],
+                         dry_tolerance=cfg.dry_tolerance, courant=cfg.courant_number, scaling=cfg.scaling,
+                         min_depth=cfg.i_min_depth, max_depth=cfg.i_max_depth)
+
+
+def cpu_baseline(grid, cfg, steps, threads):
+    """Time the OpenMP CPU step (the oracle's restatement of the reference step)
+    on the bench workload itself: `steps` steps in one call, all host threads."""
+    from oracle import oracle as O
+    m = grid.mesh
+    S = O.OmpState(m.depth, m.plotter, m.edge_cells, m.edge_local, m.bnd_cell, m.bnd_local, grid.h, grid.hu,
+                   grid.hv, grid.b, grid.r_time, grid.r_dt)
+    P = oracle_params_for(cfg)
     S.steps(P, 1, threads)  # warm-up
     t0 = time.perf_counter()
     S.steps(P, steps, threads)
@@ -184,39 +189,46 @@ def cpu_baseline(log2, steps, solver, threads):
     return m.n_cells * steps / t, t
 
 
+def basin_from_oracle(log2_cells, solver):
+    """The basin workload on the oracle's own mesh (its walk of the Sierpinski
+    grammar, oracle_mesh_uniform + oracle_mesh_edges), with the scenario's field
+    generators evaluated on the oracle's cell centroids: the CPU arm loads no
+    part of the GPU library."""
+    from oracle import oracle as O
+    from samoa_gb300 import scenarios, swe
+    om = O.mesh_uniform(log2_cells - 1)
+    c5, co = om["cells5"], om["coords"]
+    cen = ((co[:, 0] + co[:, 1]) + co[:, 2]) / 3.0
+    del om["coords"], co
+    mesh = swe.Mesh(c5[:, 1].copy(), c5[:, 2].copy(), om["edge_cells"], om["edge_local"], om["bnd_cell"],
+                    om["bnd_local"], cen)
+    return scenarios.ocean_basin(log2_cells=log2_cells, solver=solver, mesh=mesh)
+
+
 def run_reference(a, rank, world):
     if rank != 0:
         return 0
     from oracle import oracle as O
     threads = O.max_threads()
-    per_step = []
-    total_cells = 0
-    # each bench step times a bounded sample (2^cpu_sample_log2 cells) of the workload
-    from samoa_gb300 import scenarios, swe
-    scn = scenarios.ocean_basin(log2_cells=a.cpu_sample_log2, solver=a.solver)
+    scn = basin_from_oracle(a.log2_cells, a.solver)
     g = scn.grid
     m = g.mesh
     S = O.OmpState(m.depth, m.plotter, m.edge_cells, m.edge_local, m.bnd_cell, m.bnd_local, g.h, g.hu, g.hv, g.b,
                    g.r_time, g.r_dt)
-    cfg = scn.cfg
-    P = O.make_params(solver=swe.SOLVERS[cfg.flux_solver], bc=swe.BOUNDARIES[cfg.boundary],
-                      dry_tolerance=cfg.dry_tolerance, courant=cfg.courant_number, scaling=cfg.scaling,
-                      min_depth=cfg.i_min_depth, max_depth=cfg.i_max_depth)
+    P = oracle_params_for(scn.cfg)
     S.steps(P, a.warmup, threads)
     t0 = time.perf_counter()
-    for _ in range(a.steps):
-        S.steps(P, 1, threads)
-        total_cells += m.n_cells
+    S.steps(P, a.steps, threads)  # the K steps in one call, as the reference's run loop does
     t = time.perf_counter() - t0
-    value = total_cells / t
-    sample = "2^%d-cell sample of the basin workload per step (%d cells), %d steps, OpenMP C restatement" % (
-        a.cpu_sample_log2, m.n_cells, a.steps)
+    value = m.n_cells * a.steps / t
+    sample = ("the whole workload: %d cells, %d steps in one call after %d warm-up steps, OpenMP C restatement "
+              "of the reference step on the oracle's own mesh" % (m.n_cells, a.steps, a.warmup))
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1000.0 * t / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": "ocean_basin_2^%d_cells_fwave_fp64" % a.log2_cells, "solver": a.solver,
-                   "sample_cells": m.n_cells},
+        "config": {"workload": "ocean_basin_2^%d_cells_%s_fp64" % (a.log2_cells, a.solver), "cells": m.n_cells,
+                   "solver": a.solver, "boundary": "outflow"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                          "host": host_cpu()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -245,65 +257,155 @@ def fp64_dgemm_tflops(torch):
     return best
 
 
+def _time_batched(meshes, grids, cfgs, K, stream, device):
+    """Seconds of K steps of the batched ensemble (one launch per step for all
+    instances, replayed as a CUDA graph), after a warm-up replay."""
+    import torch
+
+    from samoa_gb300 import swe
+    cat = lambda k: np.concatenate([getattr(g, k) for g in grids])
+    batched = swe.SweEnsemble(device)
+    try:
+        batched.upload_meshes(meshes)
+        batched.set_params_list([c.params() for c in cfgs])
+        batched.upload_state(cat("h"), cat("hu"), cat("hv"), cat("b"))
+        batched.set_times([0.0] * len(grids), [g.r_dt for g in grids])
+        batched.set_stream(stream.cuda_stream)
+        batched.traverse_graph(K)  # capture + warm-up
+        batched.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batched.traverse_graph(K)
+        e1.record(stream)
+        e1.synchronize()
+        batched.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+    finally:
+        batched.close()
+
+
+def _time_looped(meshes, grids, cfgs, K, stream, device):
+    """Seconds of K steps of the plain step launched per instance, one context per
+    instance, all on one stream, after one warm-up step each."""
+    import torch
+
+    from samoa_gb300 import swe
+    ctxs = []
+    try:
+        for m, g, c in zip(meshes, grids, cfgs):
+            x = swe.SweContext(device)
+            ctxs.append(x)
+            x.set_params(c.params())
+            x.upload_mesh(m)
+            x.upload_state(g.h, g.hu, g.hv, g.b)
+            x.set_time(0.0, g.r_dt)
+            x.set_stream(stream.cuda_stream)
+        for x in ctxs:
+            x.traverse(1)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(K):
+            for x in ctxs:
+                x.traverse(1)
+        e1.record(stream)
+        e1.synchronize()
+        for x in ctxs:
+            x.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+    finally:
+        for x in ctxs:
+            x.close()
+
+
 def ensemble_compare(a, device):
     """Batched ensemble (one launch per step for all instances, replayed as a
     CUDA graph) against looping the plain step over the same instances (one
-    context per instance, all on one stream), same GPU, same steps."""
+    context per instance, all on one stream), same GPU, same steps; then the
+    same comparison per log2-size bucket of the instances."""
     import torch
 
-    from samoa_gb300 import scenarios, swe
+    from samoa_gb300 import scenarios
     ens = scenarios.bowl_ensemble(n_instances=a.ensemble_instances, seed=4, device="cuda")
     cells = int(sum(m.n_cells for m in ens.meshes))
     K = a.ensemble_steps
     stream = torch.cuda.Stream(device=device)
-    cat = lambda k: np.concatenate([getattr(g, k) for g in ens.grids])
-
-    batched = swe.SweEnsemble(device)
-    batched.upload_meshes(ens.meshes)
-    batched.set_params_list([c.params() for c in ens.cfgs])
-    batched.upload_state(cat("h"), cat("hu"), cat("hv"), cat("b"))
-    batched.set_times([0.0] * len(ens.grids), [g.r_dt for g in ens.grids])
-    batched.set_stream(stream.cuda_stream)
-    batched.traverse_graph(K)  # capture + warm-up
-    batched.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    batched.traverse_graph(K)
-    e1.record(stream)
-    e1.synchronize()
-    batched.synchronize()
-    t_batched = e0.elapsed_time(e1) * 1e-3
-    batched.close()
-
-    ctxs = []
-    for m, g, c in zip(ens.meshes, ens.grids, ens.cfgs):
-        x = swe.SweContext(device)
-        x.set_params(c.params())
-        x.upload_mesh(m)
-        x.upload_state(g.h, g.hu, g.hv, g.b)
-        x.set_time(0.0, g.r_dt)
-        x.set_stream(stream.cuda_stream)
-        ctxs.append(x)
-    for x in ctxs:
-        x.traverse(1)  # warm-up
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(K):
-        for x in ctxs:
-            x.traverse(1)
-    e1.record(stream)
-    e1.synchronize()
-    t_loop = e0.elapsed_time(e1) * 1e-3
-    for x in ctxs:
-        x.synchronize()
-        x.close()
+    t_batched = _time_batched(ens.meshes, ens.grids, ens.cfgs, K, stream, device)
+    t_loop = _time_looped(ens.meshes, ens.grids, ens.cfgs, K, stream, device)
     v_b = cells * K / t_batched
     v_l = cells * K / t_loop
+    buckets = {}
+    Kb = a.ensemble_bucket_steps
+    sizes = np.array([m.n_cells for m in ens.meshes])
+    for k in sorted(set(int(x).bit_length() - 1 for x in sizes)):
+        idx = [i for i in range(len(sizes)) if sizes[i] == 1 << k]
+        sel = lambda xs: [xs[i] for i in idx]
+        c = int(sizes[idx].sum())
+        tb = _time_batched(sel(ens.meshes), sel(ens.grids), sel(ens.cfgs), Kb, stream, device)
+        tl = _time_looped(sel(ens.meshes), sel(ens.grids), sel(ens.cfgs), Kb, stream, device)
+        buckets["2^%d" % k] = {"instances": len(idx), "cells": c, "batched": c * Kb / tb, "looped": c * Kb / tl,
+                               "speedup": tl / tb, "looped_ms_per_step": 1e3 * tl / Kb,
+                               "batched_ms_per_step": 1e3 * tb / Kb}
     return {"instances": len(ens.grids), "cells": cells, "steps": K, "batched": v_b, "looped": v_l,
-            "speedup": v_b / v_l, "unit": UNIT,
+            "speedup": v_b / v_l, "unit": UNIT, "batched_ms_per_step": 1e3 * t_batched / K,
+            "looped_ms_per_step": 1e3 * t_loop / K, "per_size": {"steps": Kb, "buckets": buckets},
             "note": "bowl ensemble, 2^12..2^20 cells per instance, f-wave, own dt per instance; batched = one "
                     "launch per step for all instances replayed as a CUDA graph; looped = the plain step launched "
-                    "per instance on one stream"}
+                    "per instance on one stream; per_size: the same comparison for the instances of each size "
+                    "alone"}
+
+
+def rest_edge_fraction(mesh, h, hu, hv, b, drytol):
+    """The share of inner edges whose two cells hold water at rest under one
+    surface (both momenta +-0 on both sides, both depths above the dry
+    tolerance, ((bR + dR) - bL) - dL == 0): the edges the f-wave step resolves
+    by its exact lake-at-rest path. Host numpy on the state after the run."""
+    ec = mesh.edge_cells
+    frac, n = 0, len(ec)
+    for s in range(0, n, 1 << 24):
+        e = ec[s:s + (1 << 24)]
+        L, R = e[:, 0], e[:, 1]
+        dL, dR = h[L] - b[L], h[R] - b[R]
+        still = (hu[L] == 0) & (hv[L] == 0) & (hu[R] == 0) & (hv[R] == 0)
+        wet = (dL > drytol) & (dR > drytol)
+        surf = ((b[R] + dR) - b[L]) - dL
+        frac += int(np.count_nonzero(still & wet & (surf == 0)))
+    return frac / max(n, 1)
+
+
+def moving_water(a, device):
+    """The step's rate where the water moves: the wet/dry parabolic bowl with a
+    2 m Gaussian bump (2^22 cells, f-wave, 20 steps after 3 warm-up steps), where
+    few edges are at rest, against the headline workload's rate."""
+    import torch
+
+    from samoa_gb300 import scenarios, swe
+    scn = scenarios.parabolic_bowl(log2_cells=a.moving_log2_cells, solver=a.solver, amplitude=2.0, sigma=0.08)
+    g = scn.grid
+    ctx = swe.SweContext(device)
+    try:
+        ctx.set_params(scn.cfg.params())
+        ctx.upload_mesh(g.mesh)
+        ctx.upload_state(g.h, g.hu, g.hv, g.b)
+        ctx.set_time(0.0, g.r_dt)
+        stream = torch.cuda.Stream(device=device)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.traverse(3)
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.traverse(20)
+        e1.record(stream)
+        e1.synchronize()
+        ctx.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        h, hu, hv, b = ctx.download_state()
+        rest = rest_edge_fraction(g.mesh, h, hu, hv, b, scn.cfg.dry_tolerance)
+    finally:
+        ctx.close()
+    return {"workload": "parabolic_bowl_2^%d_cells_%s_fp64" % (a.moving_log2_cells, a.solver),
+            "value": g.mesh.n_cells * 20 / t, "unit": UNIT, "steps": 20, "rest_edge_fraction": rest,
+            "note": "half of the bowl is dry land, the wet half moves"}
 
 
 def adaptive_compare(a, device):
@@ -569,6 +671,9 @@ def run_gpu(a, rank, world, local):
         dist.barrier()
     sim_time, dt, _ = ctx.get_time()
     value = n * a.steps * world / (ms * 1e-3)
+    hst = ctx.download_state()
+    rest_frac = rest_edge_fraction(g.mesh, *hst, scn.cfg.dry_tolerance) if a.solver == "fwave" else None
+    del hst
 
     # end to end through the public API with host buffers. Headline: swe_step_host,
     # the step reading the state from pinned host memory and writing the new state
@@ -636,10 +741,10 @@ def run_gpu(a, rank, world, local):
         if world == 1 and not a.no_cpu:
             from oracle import oracle as O
             threads = O.max_threads()
-            v, t = cpu_baseline(a.cpu_sample_log2, a.cpu_steps, a.solver, threads)
+            v, t = cpu_baseline(g, scn.cfg, a.cpu_steps, threads)
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "host": host_cpu(),
-                   "sample": "2^%d-cell sample of the same basin, %d steps (%.1f s), OpenMP C restatement of the "
-                             "reference step" % (a.cpu_sample_log2, a.cpu_steps, t)}
+                   "sample": "the whole workload (%d cells), %d steps in one call (%.1f s), OpenMP C restatement "
+                             "of the reference step" % (n, a.cpu_steps, t)}
         ensemble = None
         if world == 1 and not a.no_ensemble:
             try:
@@ -652,6 +757,12 @@ def run_gpu(a, rank, world, local):
                 adaptive = adaptive_compare(a, local)
             except Exception as exc:
                 adaptive = {"error": repr(exc)[:300]}
+        moving = None
+        if world == 1 and a.solver == "fwave" and not a.no_moving:
+            try:
+                moving = moving_water(a, local)
+            except Exception as exc:
+                moving = {"error": repr(exc)[:300]}
         adj = None
         if world == 1 and not a.no_adjoint:
             try:
@@ -682,6 +793,8 @@ def run_gpu(a, rank, world, local):
                 "source": "instr_per_cell from the ncu summary in profiles/, peak from the DGEMM measured above"},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "rest_edge_fraction": rest_frac,
+            "moving_water": moving,
             "ensemble": ensemble,
             "adjoint": adj,
             "adaptive": adaptive,

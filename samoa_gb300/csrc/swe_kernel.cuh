@@ -397,14 +397,16 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         double* sh_hv = sh_hu + T;
         double* sh_b = sh_hv + T;
         for (int i = tid; i < cn; i += blockDim.x) {
-            // depth_terms, with the square root and reciprocal skipped by warps of dry cells
+            // depth_terms, with the square root and reciprocal skipped by warps of dry cells.
+            // The f-wave path divides only the cell's own (rotated) momenta by its depth:
+            // with both momenta +-0 every such quotient is a zero with the numerator's
+            // sign for any positive reciprocal, so those cells skip RN(1 / d) (1.0 stands in)
             const double d = sh_h[i] - sh_b[i];
             const bool wet = lt(P.drytol, d);
-            double sq = 0.0, y = 0.0;
-            if (__any_sync(__activemask(), wet)) {
-                sq = wet ? sqrt(kG * d) : 0.0;
-                y = wet ? recip_rn(d).y : 0.0;
-            }
+            const bool need_y = wet && (SOLVER != FWAVE || ((dbits(sh_hu[i]) | dbits(sh_hv[i])) << 1) != 0);
+            double sq = 0.0, y = wet ? 1.0 : 0.0;
+            if (__any_sync(__activemask(), wet)) sq = wet ? sqrt(kG * d) : 0.0;
+            if (__any_sync(__activemask(), need_y)) y = need_y ? recip_rn(d).y : y;
             sh_rh[i] = y;
             sh_sq[i] = sq;
         }
@@ -508,18 +510,20 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             const int di = d - P.dmin;
             const double leg = tab_leg[di], hyp = tab_hyp[di], ndv = tab_ndv[di];
             double u[4][3];
-            long long nz = 0;
+            long long nz = 0, sz = 0;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 u[q][0] = upd[(q * 3 + k0) * T + i];
                 u[q][1] = upd[(q * 3 + 1) * T + i];
                 u[q][2] = upd[(q * 3 + k2) * T + i];
-                nz |= (dbits(u[q][0]) | dbits(u[q][1]) | dbits(u[q][2])) << 1;
+                (q < 3 ? nz : sz) |= (dbits(u[q][0]) | dbits(u[q][1]) | dbits(u[q][2])) << 1;
             }
-            // quiet: every edge update is +-0 (dry land, water at rest). Then each sum
-            // below is +0 (positive edge lengths), RN(ndv * +0) is a zero with ndv's sign,
-            // and adding it leaves the state as add_zero says: the same bits, without
-            // the FP64 arithmetic.
+            // quiet: every update of h, hu, hv is +-0 (dry land, water at rest). Then
+            // each sum below is +0 (positive edge lengths), RN(ndv * +0) is a zero with
+            // ndv's sign, and adding it leaves the state as add_zero says: the same
+            // bits, without the FP64 arithmetic. The speed sum ds is +0 when every
+            // speed is +-0 (dry land), else it is summed (water at rest still has
+            // wave speeds).
             const bool quiet = nz == 0 && is_finite(ndv);
             double dh = 0.0, dp1 = 0.0, dp2 = 0.0, ds = 0.0;
             if (__any_sync(__activemask(), !quiet)) {
@@ -530,6 +534,10 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
                     dp1 = dp1 + imul_cell(leg, u[1][2]);
                     dp2 = z0(imul_cell(leg, u[2][0])) + imul_cell(hyp, u[2][1]);
                     dp2 = dp2 + imul_cell(leg, u[2][2]);
+                }
+            }
+            if (__any_sync(__activemask(), sz != 0)) {
+                if (sz != 0) {
                     ds = z0(imul_cell(leg, u[3][0])) + imul_cell(hyp, u[3][1]);
                     ds = ds + imul_cell(leg, u[3][2]);
                 }

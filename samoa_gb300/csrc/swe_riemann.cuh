@@ -740,6 +740,38 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         fR = Update{0.0, 0.0, 0.0, 0.0};
         return;
     }
+    if (SOLVER == FWAVE && FZ == 0) {
+        // Water at rest on both sides under one surface (lake at rest): every
+        // momentum is +-0, both sides are wet and the c-binding's surface
+        // difference ((bR + hR) - bL) - hL is +-0. Then in the f-wave path the
+        // velocities, uhat and the momentum jump are signed zeros; delphi is
+        // +-0 - X with X = RN(ghalf_h (bR - bL)) and deldelphi is -X, so
+        // delphi - deldelphi is a zero (x - x = +0), both f-wave coefficients
+        // divide a zero, and every f-wave component is a signed zero. The net
+        // updates start at +0 and add zeros, so they are +0, and rotating them
+        // back gives +0 in every component. The speeds are sL = -sqL,
+        // sR = sqR, Roe uhat -+ chat = -+chat with chat = sqrt(ghalf_h), so
+        // |sE1| = max(sqL, chat), |sE2| = max(sqR, chat), and the middle wave's
+        // |RN(sE1 + sE2) / 2| (sE1 <= 0 <= sE2) exceeds neither: the maximum
+        // speed is the largest of sqL, sqR and chat. And chat never exceeds
+        // the larger of sqL, sqR: with h the larger depth, RN(hR + hL) <= 2h,
+        // so ghalf_h = RN(RN(g / 2) RN(hR + hL)) <= RN((g / 2) 2h) = RN(g h)
+        // (g / 2 is exact, and RN, the product by a positive factor and sqrt
+        // are monotone), hence chat <= RN(sqrt(RN(g h))), the cell's own
+        // sqrt(g h). So the maximum speed is max(sqL, sqR), both positive. The
+        // same bits as the full evaluation, without its FP64 arithmetic.
+        const bool still = ((dbits(QL.p1) | dbits(QL.p2) | dbits(QR.p1) | dbits(QR.p2)) << 1) == 0;
+        if (still && lt(drytol, dL) && lt(drytol, dR)) {
+            const double surf = ((QR.b + dR) - QL.b) - dL;
+            if ((dbits(surf) << 1) == 0) {
+                const long long m = dbits(sqL) > dbits(sqR) ? dbits(sqL) : dbits(sqR);
+                const double ms = bitsd(m);
+                fL = Update{0.0, 0.0, 0.0, ms};
+                fR = Update{0.0, 0.0, 0.0, ms};
+                return;
+            }
+        }
+    }
     const bool fin = is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
     const bool fast = axis != 0 && fin;
     const bool diag = axis == 0 && fin && abs_bits(n1) == abs_bits(n2);

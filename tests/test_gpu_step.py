@@ -203,6 +203,33 @@ def test_lake_at_rest_is_exact(swe_lib):
         trav.close()
 
 
+@pytest.mark.parametrize("boundary", ["outflow", "slip", "noslip"])
+def test_rest_edges_bitexact(swe_lib, oracle_lib, boundary):
+    """The f-wave step's lake-at-rest path (both sides wet, every momentum +-0,
+    ((bR + dR) - bL) - dL a zero) against the oracle walk: a lake at rest over
+    rough bathymetry where a quarter of the cells hold -0 momenta, some
+    surfaces are one ulp off (their edges take the full path), some cells are
+    dry land and one patch moves, so rest edges border moving and dry ones."""
+    scn = scenarios.lake_at_rest(log2_cells=12)
+    scn.cfg.boundary = boundary
+    g = scn.grid
+    n = g.mesh.n_cells
+    rng = np.random.default_rng(42)
+    neg = rng.random(n) < 0.25
+    g.hu[neg] = -0.0
+    g.hv[rng.random(n) < 0.25] = -0.0
+    ulp = rng.random(n) < 0.05
+    g.h[ulp] = np.nextafter(g.h[ulp], 1.0)
+    dry = rng.random(n) < 0.03
+    g.b[dry] = 0.5
+    g.h[dry] = 0.0  # surface min(b, 0) on dry land
+    patch = np.arange(n // 3, n // 3 + 64)
+    g.hu[patch] = 0.3
+    g.hv[patch] = -0.2
+    g.r_dt = swe.initial_dt(g.mesh, g.h, g.hu, g.hv, g.b, scn.cfg.courant_number)
+    run_compare_walk(scn, 12)
+
+
 @pytest.mark.parametrize("solver", ["fwave", "aug_riemann", "llfbath"])
 def test_all_dry_domain(swe_lib, oracle_lib, solver):
     """Dry land everywhere (surface at min(b, 0) below a positive bottom): no edge
