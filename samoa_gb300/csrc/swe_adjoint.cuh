@@ -404,6 +404,37 @@ __device__ __forceinline__ void geoclaw_vjp(double n1, double n2, const State& Q
                                             Grad4& outR, int axis = 0) {
     const double g = kG;
     const double c = 0.5 * g;
+    if (SOLVER == FWAVE) {
+        // Water at rest on both sides under one surface (the forward step's
+        // lake-at-rest path: every momentum +-0, both sides wet, the surface
+        // difference ((bR + dR) - bL) - dL a zero). There beta1 = beta2 = 0 and
+        // every velocity is 0, so to first order only the coefficients move:
+        // d beta1 = (sE2 d delhu - d dpd) / D, d beta2 = (d dpd - sE1 d delhu) / D
+        // (D = sE2 - sE1; the derivatives through sE1, sE2 and D multiply a zero),
+        // d dpd = ghalf_h (d hR' - d hL') with h' the surfaces (the surface
+        // difference multiplies the zero, and b cancels between delphi and
+        // deldelphi), d delhu = n . (d pR - d pL). The left net update is
+        // beta1 (1, sE1 n) (sE1 < 0), the right one beta2 (1, sE2 n) (sE2 > 0);
+        // the middle wave's components are products of two zeros.
+        const bool still = ((dbits(QL.p1) | dbits(QL.p2) | dbits(QR.p1) | dbits(QR.p2)) << 1) == 0;
+        if (still && lt(drytol, dL0) && lt(drytol, dR0) && (dbits(((QR.b + dR0) - QL.b) - dL0) << 1) == 0) {
+            const double ghalf = c * (dR0 + dL0);
+            const double chat = sqrt(ghalf);
+            const double sE1 = -imax(sqL0, chat), sE2 = imax(sqR0, chat);
+            const double rD = rcp_nr(sE2 - sE1);
+            const double gb1 = gL[0] + sE1 * (n1 * gL[1] + n2 * gL[2]);
+            const double gb2 = gR[0] + sE2 * (n1 * gR[1] + n2 * gR[2]);
+            const double g_du = (sE2 * gb1 - sE1 * gb2) * rD;  // cotangent of delhu
+            const double g_dh = ghalf * ((gb2 - gb1) * rD);    // of hR' (minus it for hL')
+            outL.h -= g_dh;
+            outR.h += g_dh;
+            outL.hu -= g_du * n1;
+            outL.hv -= g_du * n2;
+            outR.hu += g_du * n1;
+            outR.hv += g_du * n2;
+            return;
+        }
+    }
     // ---------------- forward (geoclaw_flux<SOLVER>, the same values)
     const bool fin = is_finite(QL.p1) && is_finite(QL.p2) && is_finite(QR.p1) && is_finite(QR.p2);
     const bool fast = axis != 0 && fin;

@@ -281,6 +281,10 @@ struct swe_ctx {
     int64_t dt_seq_len = 0;
     std::vector<double> dt_seq_host;
     uint8_t* branch = nullptr;      // wet/dry branch flags of the last forward step (adjoint)
+    // per cell (d, sqrt(g d)) of the last depth the step kernel took a square root of: a
+    // cache of a function of d (any entry is a valid pair, so nothing ever invalidates it;
+    // all bits set, a NaN key, when allocated)
+    double2* memo = nullptr;
     // allocated sizes (elements) of the per-cell, per-instance and task buffers: a re-upload that
     // fits reuses them, so remeshing every step does not pay cudaMalloc / cudaFree each time
     size_t cap_cells = 0, cap_inst = 0, cap_tasks = 0, cap_segs = 0, cap_xtasks = 0;
@@ -325,6 +329,8 @@ void free_mesh_buffers(swe_ctx* c, bool release = true) {
     }
     cudaFree(c->b); cudaFree(c->depth); cudaFree(c->flags); cudaFree(c->tasks); cudaFree(c->seg_ptr);
     cudaFree(c->seg_info); cudaFree(c->seg_order); cudaFree(c->ip); cudaFree(c->is); cudaFree(c->xtasks); cudaFree(c->xflux);
+    cudaFree(c->memo);
+    c->memo = nullptr;
     c->b = nullptr; c->depth = nullptr; c->flags = nullptr; c->tasks = nullptr; c->seg_ptr = nullptr;
     c->seg_info = nullptr; c->seg_order = nullptr; c->ip = nullptr; c->is = nullptr; c->xtasks = nullptr; c->xflux = nullptr;
     c->n_xtasks = 0;
@@ -589,12 +595,14 @@ int upload_meshes(swe_ctx* c, int64_t ni, const int64_t* n_cells, const int64_t*
                 (rc = device_alloc((void**)&c->hv[k], cap * 8)))
                 break;
         if (!rc && !(rc = device_alloc((void**)&c->b, cap * 8)) && !(rc = device_alloc((void**)&c->depth, cap)) &&
-            !(rc = device_alloc((void**)&c->flags, cap)) && !(rc = device_alloc((void**)&c->ip, sizeof(InstParams) * capi)))
+            !(rc = device_alloc((void**)&c->flags, cap)) && !(rc = device_alloc((void**)&c->ip, sizeof(InstParams) * capi)) &&
+            !(rc = device_alloc((void**)&c->memo, cap * sizeof(double2))))
             rc = device_alloc((void**)&c->is, sizeof(InstScalars) * capi);
         if (rc) {
             free_mesh_buffers(c);
             return rc;
         }
+        CUDA_TRY(cudaMemsetAsync(c->memo, 0xff, cap * sizeof(double2), c->stream));
         c->cap_cells = cap;
         c->cap_inst = capi;
     }
@@ -690,6 +698,7 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
     // fault injection (tests): the staging barrier expects 16 bytes that no copy
     // delivers, so its phase never completes and the bounded wait, shortened to
     // 20 ms, gives up; every issued copy still lands before the CTA leaves
+    A.memo = c->memo;
     A.extra_tx = c->inject == SWE_INJECT_STAGING_TX ? 16u : 0u;
     A.wait_ns = c->inject == SWE_INJECT_STAGING_TX ? 20000000ull : kWaitNs;
     // edges between two segments: a pass before the step kernel for device-resident
