@@ -172,9 +172,10 @@ class GaugeProblem:
             self.stats["forward_steps"] += 1
 
     # ---- objective
-    def objective(self, h0, b, record=True):
-        """J and the gauge series h_{t+1}[g] of a forward run."""
-        self._set_initial(h0, b)
+    def objective(self, h0, b, record=True, hu0=None, hv0=None):
+        """J and the gauge series h_{t+1}[g] of a forward run (initial momenta
+        hu0, hv0; at rest by default)."""
+        self._set_initial(h0, b, hu0, hv0)
         L = self.ctx.L
         with torch.cuda.stream(self.stream):
             gv = torch.empty((self.T, len(self.gauges)), dtype=torch.float64, device=self.dev)

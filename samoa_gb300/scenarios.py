@@ -276,6 +276,27 @@ def ocean_basin(log2_cells=26, seed=3, solver="fwave", steps=200, mesh=None, sca
     return Scenario("ocean_basin", _grid(mesh, cfg, h, b), cfg, steps)
 
 
+def current_basin(log2_cells=12, u0=2.0, v0=1.0, seed=8, mesh=None):
+    """A deep basin (100 km square, depths 80 to 120 m of smooth seeded relief)
+    under a uniform current (u0, v0) m/s with a 0.5 m Gaussian surface bump: all
+    wet, and the normal velocity is away from 0 on every edge orientation of the
+    Sierpinski mesh (axis-aligned and diagonal normals), so no wave speed sits
+    at 0. f-wave, outflow. Returns the scenario with the current's momenta set."""
+    d = log2_cells - 1
+    cfg = Config(flux_solver="fwave", boundary="outflow", courant_number=0.45, dry_tolerance=0.01, scaling=1.0e5,
+                 offset=(-0.5e5, -0.5e5), i_min_depth=d, i_max_depth=d)
+    mesh = mesh or uniform_mesh(d)
+    u, v = mesh.centroids[:, 0] - 0.5, mesh.centroids[:, 1] - 0.5
+    b = -100.0 + 20.0 * value_noise(u, v, seed, octaves=2, base=3.0)
+    h = 0.5 * np.exp(-(u * u + v * v) / (2 * 0.1 * 0.1))
+    g = _grid(mesh, cfg, h, b)
+    depth = g.h - g.b
+    g.hu[:] = depth * u0
+    g.hv[:] = depth * v0
+    g.r_dt = initial_dt(mesh, g.h, g.hu, g.hv, g.b, cfg.courant_number)
+    return Scenario("current_basin", g, cfg, 100)
+
+
 def lake_at_rest(log2_cells=10, solver="fwave", seed=7, mesh=None):
     """Flat surface at 0 over rough bathymetry, at rest: the well-balanced solvers keep it exactly."""
     d = log2_cells - 1
