@@ -466,6 +466,9 @@ __device__ __forceinline__ void geoclaw_vjp(double n1, double n2, const State& Q
     const bool wetR = lt(drytol, hR), wetL = lt(drytol, hL);
     if (!wetL && !wetR && !is_nan(hL) && !is_nan(hR)) return;  // no flux, no derivative
     double huL, huR, uL, uR, vL, vR;
+    // a wet cell whose reciprocal was left for the edges that need it (f-wave, zero momenta)
+    if (SOLVER == FWAVE && wetR && dbits(yR0) == 0) yR0 = recip_rn(hR).y;
+    if (SOLVER == FWAVE && wetL && dbits(yL0) == 0) yL0 = recip_rn(hL).y;
     if (wetR) {
         const Recip r{hR, yR0, recip_fast(hR)};
         huR = pR1; uR = div_rn(pR1, r); vR = div_rn(pR2, r);
@@ -893,6 +896,7 @@ struct AdjointArgs {
     double dt;
     int32_t n_seg, seg_cells, n_cells_total, parity;
     unsigned int* error;
+    double2* memo;            // per cell (d, sqrt(g d)) shared with the forward step, or null
 };
 
 // mu = -dt / volume * lambda' where the drying clamp did not fire: the
@@ -944,9 +948,29 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
             sh_hu[i] = A.hu[cc];
             sh_hv[i] = A.hv[cc];
             sh_b[i] = b;
-            double d, sq, y;
-            depth_terms(State{h, 0.0, 0.0, b}, P.drytol, d, sq, y);
-            sh_rh[i] = y;
+            // sqrt(g d) from the step's memo when the depth has the same bits (a
+            // pair (d, sqrt(g d)) either way, so a hit is the root's value; a miss
+            // is written back by this CTA, which owns the cell). The f-wave's
+            // RN(1 / d) is left to the VJP of an edge that takes the general path
+            // (0 here) when the cell's momenta are +-0, since its edges may all be
+            // at rest; a cell with momentum has general edges and gets it here.
+            const double d = h - b;
+            const bool wet = lt(P.drytol, d);
+            double sq = 0.0;
+            bool miss = wet;
+            if (wet && A.memo) {
+                const double2 m = A.memo[cc];
+                if (dbits(m.x) == dbits(d)) {
+                    sq = m.y;
+                    miss = false;
+                }
+            }
+            if (miss) {
+                sq = sqrt(kG * d);
+                if (A.memo) A.memo[cc] = make_double2(d, sq);
+            }
+            const bool still = ((dbits(sh_hu[i]) | dbits(sh_hv[i])) << 1) == 0;
+            sh_rh[i] = (wet && (SOLVER != FWAVE || !still)) ? recip_rn(d).y : 0.0;
             sh_sq[i] = sq;
             const int dd = A.depth[cc];
             const double vol = (P.scaling * P.scaling) * c_vol[dd];

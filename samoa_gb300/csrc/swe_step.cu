@@ -161,12 +161,29 @@ __global__ void gauge_kernel(const GlobalScalars* G, const double* h0, const dou
     }
 }
 
-// lam_h[gauge g] += 2 (value[g] - obs[g]) for the gauges in order (one thread:
-// a gauge listed twice adds twice, as in sequence)
+// lam_h[gauge g] += 2 (value[g] - obs[g]) for the gauges in order: a gauge listed
+// twice adds twice, in list order. Up to kResidualParallel gauges, the thread of
+// a cell's first listing adds all of its listings in list order (the same sums
+// in the same order as one thread walking the list, without its chain of
+// dependent loads); beyond that, one thread walks the list.
+constexpr int64_t kResidualParallel = 4096;
 __global__ void gauge_residual_kernel(double* lam_h, const int64_t* cells, int64_t n, const double* value,
                                       const double* obs) {
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        for (int64_t i = 0; i < n; ++i) lam_h[cells[i]] += 2.0 * (value[i] - obs[i]);
+    if (n > kResidualParallel) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            for (int64_t i = 0; i < n; ++i) lam_h[cells[i]] += 2.0 * (value[i] - obs[i]);
+        return;
+    }
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const int64_t c = cells[i];
+        bool first = true;
+        for (int64_t j = 0; j < i && first; ++j) first = cells[j] != c;
+        if (!first) continue;
+        double acc = lam_h[c];
+        for (int64_t j = i; j < n; ++j)
+            if (cells[j] == c) acc += 2.0 * (value[j] - obs[j]);
+        lam_h[c] = acc;
+    }
 }
 
 // J = sum over all entries of (value - obs)^2, one block, fixed order per thread
@@ -1329,6 +1346,7 @@ int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double*
     A.n_cells_total = (int32_t)c->cells_total;
     A.parity = (int32_t)(t & 1);
     A.error = &c->gs->error;
+    A.memo = c->memo;
     // the reverse kernel holds more registers per thread than the step: it runs
     // 256 threads per CTA so an SM still has two CTAs' worth of warps
     const int threads = 256;
@@ -1634,8 +1652,8 @@ struct Sweep {
         }
         double** in = lam[li];
         double** out = lam[li ^ 1];
-        gauge_residual_kernel<<<1, 32, 0, c->stream>>>(in[0], gauges, G, gv + (size_t)t * (size_t)G,
-                                                       obs + (size_t)t * (size_t)G);
+        gauge_residual_kernel<<<1, (unsigned)std::min<int64_t>(std::max<int64_t>(G, 32), 256), 0, c->stream>>>(
+            in[0], gauges, G, gv + (size_t)t * (size_t)G, obs + (size_t)t * (size_t)G);
         CUDA_TRY(cudaGetLastError());
         int r = launch_adjoint(c, s0 + t, branches + (size_t)t * (size_t)stride, in[0], in[1], in[2], out[0],
                                out[1], out[2], bbar);
