@@ -897,6 +897,11 @@ struct AdjointArgs {
     int32_t n_seg, seg_cells, n_cells_total, parity;
     unsigned int* error;
     double2* memo;            // per cell (d, sqrt(g d)) shared with the forward step, or null
+    // per depth d: -dt / volume(d) and scaling * sqrt(0.5)^(d - 1) (edge lengths: the
+    // hypotenuse of a depth-d cell is len[d], its legs len[d + 1]), computed on the host
+    // with the same operations the cells would do, once per launch
+    double ndv_tab[kMaxDepth + 1];
+    double len_tab[kMaxDepth + 2];
 };
 
 // mu = -dt / volume * lambda' where the drying clamp did not fire: the
@@ -973,9 +978,8 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
             sh_rh[i] = (wet && (SOLVER != FWAVE || !still)) ? recip_rn(d).y : 0.0;
             sh_sq[i] = sq;
             const int dd = A.depth[cc];
-            const double vol = (P.scaling * P.scaling) * c_vol[dd];
             double m0, m1, m2;
-            cell_mu(A, cc, -A.dt / vol, m0, m1, m2);
+            cell_mu(A, cc, A.ndv_tab[dd], m0, m1, m2);
             sh_mu[i] = m0;
             sh_mu[T + i] = m1;
             sh_mu[2 * T + i] = m2;
@@ -1018,7 +1022,7 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                 QL = State{A.h[L], A.hu[L], A.hv[L], A.b[L]};
                 depth_terms(QL, P.drytol, dL, sqL, yL);
                 const int dd = A.depth[L];
-                cell_mu(A, L, -A.dt / ((P.scaling * P.scaling) * c_vol[dd]), mL[0], mL[1], mL[2]);
+                cell_mu(A, L, A.ndv_tab[dd], mL[0], mL[1], mL[2]);
             }
             depL = A.depth[L];
             if (bnd) {
@@ -1039,16 +1043,16 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                     QR = State{A.h[R], A.hu[R], A.hv[R], A.b[R]};
                     depth_terms(QR, P.drytol, dR, sqR, yR);
                     const int dd = A.depth[R];
-                    cell_mu(A, R, -A.dt / ((P.scaling * P.scaling) * c_vol[dd]), mR[0], mR[1], mR[2]);
+                    cell_mu(A, R, A.ndv_tab[dd], mR[0], mR[1], mR[2]);
                 }
                 depR = A.depth[R];
             }
             // the edge's length in each cell: hypotenuse for local edge 2, else a leg
-            const double lenL = P.scaling * c_leg[iL == 1 ? depL : depL + 1];
+            const double lenL = A.len_tab[iL == 1 ? depL : depL + 1];
             const double gL[3] = {lenL * mL[0], lenL * mL[1], lenL * mL[2]};
             double gR[3] = {0.0, 0.0, 0.0};
             if (!bnd) {
-                const double lenR = P.scaling * c_leg[iR == 1 ? depR : depR + 1];
+                const double lenR = A.len_tab[iR == 1 ? depR : depR + 1];
                 gR[0] = lenR * mR[0];
                 gR[1] = lenR * mR[1];
                 gR[2] = lenR * mR[2];

@@ -640,7 +640,9 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     double sqR = wetR ? (wall_r ? sqL0 : sqR0) : 0.0;
     double sL = uL - sqL;
     double sR = uR + sqR;
-    double uhat = div_rn(imul(sqL, uL) + imul(sqR, uR), recip_rn(sqR + sqL));
+    // one division with its own divisor: the IEEE division (correctly rounded, as
+    // recip_rn + div_rn is) needs fewer FP64 instructions than a private reciprocal
+    double uhat = (imul(sqL, uL) + imul(sqR, uR)) / (sqR + sqL);
     double chat = sqrt(ghalf_h);
     const double r1 = uhat - chat, r2 = uhat + chat;
     double sE1 = fzb<FZ>(fz, 7, lt(sL, r1)) ? sL : r1;  // imin(sL, r1)

@@ -1347,6 +1347,11 @@ int launch_adjoint(swe_ctx* c, long long t, const uint8_t* branch, const double*
     A.parity = (int32_t)(t & 1);
     A.error = &c->gs->error;
     A.memo = c->memo;
+    {
+        const double s2 = A.P.scaling * A.P.scaling;
+        for (int d = 0; d <= kMaxDepth; ++d) A.ndv_tab[d] = -A.dt / (s2 * c->vol[d]);
+        for (int d = 0; d <= kMaxDepth + 1; ++d) A.len_tab[d] = A.P.scaling * c->leg[d];
+    }
     // the reverse kernel holds more registers per thread than the step: it runs
     // 256 threads per CTA so an SM still has two CTAs' worth of warps
     const int threads = 256;
