@@ -257,7 +257,11 @@ def fp64_dgemm_tflops(torch):
     return best
 
 
-def _time_batched(meshes, grids, cfgs, K, stream, device):
+ENSEMBLE_TILINGS = [(256, 128), (384, 128), (512, 128), (512, 256)]
+E2E_TILINGS = [(384, 128, 1), (384, 128, 2), (256, 128, 2), (512, 128, 2), (512, 256, 2), (768, 256, 1)]
+
+
+def _time_batched(meshes, grids, cfgs, K, stream, device, tiling=None):
     """Seconds of K steps of the batched ensemble (one launch per step for all
     instances, replayed as a CUDA graph), after a warm-up replay."""
     import torch
@@ -266,6 +270,8 @@ def _time_batched(meshes, grids, cfgs, K, stream, device):
     cat = lambda k: np.concatenate([getattr(g, k) for g in grids])
     batched = swe.SweEnsemble(device)
     try:
+        if tiling:
+            batched.set_tiling(*tiling)
         batched.upload_meshes(meshes)
         batched.set_params_list([c.params() for c in cfgs])
         batched.upload_state(cat("h"), cat("hu"), cat("hv"), cat("b"))
@@ -330,7 +336,12 @@ def ensemble_compare(a, device):
     cells = int(sum(m.n_cells for m in ens.meshes))
     K = a.ensemble_steps
     stream = torch.cuda.Stream(device=device)
-    t_batched = _time_batched(ens.meshes, ens.grids, ens.cfgs, K, stream, device)
+    # the batched context's tiling: a short search over segment length x block size
+    # (10 steps each, untimed in the result), as the plain step's autotuner does
+    trial = {t: _time_batched(ens.meshes, ens.grids, ens.cfgs, 10, stream, device, tiling=t)
+             for t in ENSEMBLE_TILINGS}
+    best = min(trial, key=trial.get)
+    t_batched = _time_batched(ens.meshes, ens.grids, ens.cfgs, K, stream, device, tiling=best)
     t_loop = _time_looped(ens.meshes, ens.grids, ens.cfgs, K, stream, device)
     v_b = cells * K / t_batched
     v_l = cells * K / t_loop
@@ -341,13 +352,14 @@ def ensemble_compare(a, device):
         idx = [i for i in range(len(sizes)) if sizes[i] == 1 << k]
         sel = lambda xs: [xs[i] for i in idx]
         c = int(sizes[idx].sum())
-        tb = _time_batched(sel(ens.meshes), sel(ens.grids), sel(ens.cfgs), Kb, stream, device)
+        tb = _time_batched(sel(ens.meshes), sel(ens.grids), sel(ens.cfgs), Kb, stream, device, tiling=best)
         tl = _time_looped(sel(ens.meshes), sel(ens.grids), sel(ens.cfgs), Kb, stream, device)
         buckets["2^%d" % k] = {"instances": len(idx), "cells": c, "batched": c * Kb / tb, "looped": c * Kb / tl,
                                "speedup": tl / tb, "looped_ms_per_step": 1e3 * tl / Kb,
                                "batched_ms_per_step": 1e3 * tb / Kb}
     return {"instances": len(ens.grids), "cells": cells, "steps": K, "batched": v_b, "looped": v_l,
             "speedup": v_b / v_l, "unit": UNIT, "batched_ms_per_step": 1e3 * t_batched / K,
+            "batched_tiling": list(best), "tiling_trials_ms_per_step": {"%dx%d" % k: 1e2 * v for k, v in trial.items()},
             "looped_ms_per_step": 1e3 * t_loop / K, "per_size": {"steps": Kb, "buckets": buckets},
             "note": "bowl ensemble, 2^12..2^20 cells per instance, f-wave, own dt per instance; batched = one "
                     "launch per step for all instances replayed as a CUDA graph; looped = the plain step launched "
@@ -503,6 +515,10 @@ def adjoint_compare(a, device):
     finally:
         P.close()
     windowed = adjoint_windowed(a, case, device)
+    try:
+        moving_fd = adjoint_moving_fd(device)
+    except Exception as exc:
+        moving_fd = {"error": repr(exc)[:300]}
     n = case["mesh"].n_cells
     return {"cells": n, "steps": a.adjoint_steps, "snapshots": 64, "J": J, "forward_s": t_fwd, "gradient_s": t_grad,
             "gradient_over_forward": t_grad / t_fwd, "forward_steps_in_gradient": stats["forward_steps"],
@@ -516,7 +532,7 @@ def adjoint_compare(a, device):
             "fd_frozen_rel_err_b_along_gradient": fb, "fd_frozen_directions_b": len(fbr),
             "fd_frozen_max_err_over_grad_norm_b": max(fbr, default=None),
             "forward_step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj, "adjoint_step_over_forward_step": t_adj / t_step,
-            "windowed": windowed,
+            "windowed": windowed, "fd_moving_water": moving_fd,
             "note": "gradient_s = one checkpointed sweep (its first descent is the forward run; recomputation "
                     "included); J(h0, b) is the squared misfit at 32 gauges; dt frozen, FD with the same dts, "
                     "eps = 1e-6 relative, seeded N(0,1) directions on the cells deeper than 100 m. J is piecewise "
@@ -530,6 +546,47 @@ def adjoint_compare(a, device):
                     "|g| |d|: the shelf is flat, so many directional derivatives are tiny). Perturbing b "
                     "reorders neighbouring depths at rest and so crosses the Einfeldt min/max kinks over 2,000 "
                     "steps, so plain FD in b is kink-limited"}
+
+
+def adjoint_moving_fd(device, steps=100, n_dir=6):
+    """Plain central differences of J where the water moves everywhere: the
+    current basin (2^12 cells, a uniform (2, 1) m/s current over 80-120 m of
+    depth, 100 steps, frozen dt), where no wave speed sits at 0 and nothing is
+    dry, so J has no jumps. Error against the adjoint gradient in seeded
+    directions of the initial surface (momenta held)."""
+    from samoa_gb300 import adjoint, scenarios, swe
+    scn = scenarios.current_basin(log2_cells=12)
+    g = scn.grid
+    ctx = swe.SweContext(device)
+    try:
+        ctx.set_params(scn.cfg.params())
+        ctx.upload_mesh(g.mesh)
+        ctx.upload_state(g.h, g.hu, g.hv, g.b)
+        ctx.set_time(0.0, g.r_dt)
+        ctx.traverse(1)
+        _, dt, _ = ctx.get_time()
+    finally:
+        ctx.close()
+    rng = np.random.default_rng(8)
+    gauges = np.sort(rng.choice(g.mesh.n_cells, 12, replace=False))
+    obs = rng.normal(0.0, 0.05, (steps, 12))
+    P = adjoint.GaugeProblem(g.mesh, scn.cfg.params(), gauges, obs, np.full(steps, 0.8 * dt), snapshots=8,
+                             device=device)
+    try:
+        _, gh, _ = P.gradient_python(g.h, g.b, g.hu, g.hv)
+        gh = gh.cpu().numpy()
+        errs = []
+        for _ in range(n_dir):
+            d = rng.normal(size=g.mesh.n_cells)
+            eps = 1e-5 * np.abs(g.h).max()
+            Jp = P.objective(g.h + eps * d, g.b, record=False, hu0=g.hu, hv0=g.hv)
+            Jm = P.objective(g.h - eps * d, g.b, record=False, hu0=g.hu, hv0=g.hv)
+            ad = float(gh @ d)
+            errs.append(abs((Jp - Jm) / (2 * eps) - ad) / max(abs(ad), 1e-300))
+    finally:
+        P.close()
+    return {"workload": "current_basin_2^12_cells_fwave", "steps": steps, "directions_h0": n_dir,
+            "max_rel_err_h0": max(errs), "note": "plain central differences (eps 1e-5 relative), no branch freezing"}
 
 
 def adjoint_windowed(a, case, device):
@@ -689,6 +746,30 @@ def run_gpu(a, rank, world, local):
         ctx.step_host(*cur, hb, *nxt, hflags)  # warm-up
         ctx.synchronize()
         cur, nxt = nxt, cur
+        # the host-memory step's own tiling: its loads wait on the CPU-GPU link rather
+        # than on HBM, so a short search (3 steps each, untimed in the result) over
+        # segment length, block size and staging depth picks it
+        e2e_trials = {}
+        if not (a.segment_cells or a.block_threads):
+            for seg, blk, st in E2E_TILINGS:
+                try:
+                    ctx.set_staging(1)
+                    ctx.set_tiling(seg, blk)
+                    ctx.set_staging(st)
+                except Exception:
+                    continue
+                ctx.step_host(*cur, hb, *nxt, hflags)
+                ctx.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(3):
+                    ctx.step_host(*cur, hb, *nxt, hflags)
+                    ctx.synchronize()
+                e2e_trials[(seg, blk, st)] = (time.perf_counter() - t0) / 3
+            if e2e_trials:
+                seg, blk, st = min(e2e_trials, key=e2e_trials.get)
+                ctx.set_staging(1)
+                ctx.set_tiling(seg, blk)
+                ctx.set_staging(st)
         if world > 1:
             dist.barrier()
         t0 = time.perf_counter()
@@ -713,6 +794,8 @@ def run_gpu(a, rank, world, local):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             te, tc = (float(x) for x in t.tolist())
         e2e = {"value": n * a.e2e_steps * world / te, "unit": UNIT, "h2d_bytes_per_step": 32 * n,
+               "tiling": list(min(e2e_trials, key=e2e_trials.get)) if e2e_trials else None,
+               "tiling_trials_ms_per_step": {"%dx%d/s%d" % k: round(v * 1e3, 3) for k, v in e2e_trials.items()},
                "d2h_bytes_per_step": 24 * n + n, "steps": a.e2e_steps, "api": "swe_step_host",
                "note": "every step reads h, hu, hv, b from pinned host memory and writes h, hu, hv and the "
                        "refinement flags to pinned host memory inside the step kernel, then synchronises",
