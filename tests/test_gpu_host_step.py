@@ -34,15 +34,19 @@ def _resident(scn, steps):
 
 
 @pytest.mark.parametrize("where,cross", [("pinned", "auto"), ("device", "auto"), ("device_offset", "auto"),
-                                         ("pinned", "pass"), ("device", "inkernel")])
+                                         ("pinned", "pass"), ("device", "inkernel"), ("pinned_b_resident", "auto")])
 def test_host_step_matches_resident_step(swe_lib, where, cross):
+    """The step on the caller's arrays (pinned host memory, device memory, 8-byte
+    aligned device memory; b passed each step, or b = NULL: the uploaded
+    bathymetry) against the resident step, bit for bit."""
     import torch
     scn = scenarios.radial_dam_break(log2_cells=12, boundary="slip")
     g = scn.grid
     steps = 3
     ref = _resident(scn, steps)
     n = g.mesh.n_cells
-    if where == "pinned":
+    b_resident = where == "pinned_b_resident"
+    if where in ("pinned", "pinned_b_resident"):
         mk = lambda a: torch.tensor(a).pin_memory()
         buf = lambda dt: torch.zeros(n, dtype=dt).pin_memory()
     elif where == "device":
@@ -60,9 +64,11 @@ def test_host_step_matches_resident_step(swe_lib, where, cross):
         ctx.set_params(scn.cfg.params())
         ctx.upload_mesh(g.mesh)
         ctx.set_cross_pass(cross)
+        if b_resident:
+            ctx.upload_state(g.h, g.hu, g.hv, g.b)
         ctx.set_time(0.0, _dt0(scn))
         for k in range(steps):
-            ctx.step_host(*cur, b, *nxt, flags)
+            ctx.step_host(*cur, None if b_resident else b, *nxt, flags)
             ctx.synchronize()
             h, hu, hv, f, nref, tm = ref[k]
             assert np.array_equal(nxt[0].cpu().numpy(), h)
