@@ -292,12 +292,16 @@ class GaugeProblem:
 
 def time_steps(problem, h0, b, k=50):
     """Seconds per forward step and per reverse step (the adjoint kernel with
-    recorded branches), on the problem's mesh, from the state (h0, b)."""
+    recorded branches), on the problem's mesh, from the state (h0, b). The
+    reverse steps take seeded random cotangents on every cell (a zero
+    cotangent lets the kernel skip an edge, which would not time the reverse)."""
     P = problem
     L = P.ctx.L
     P._set_initial(h0, b)
     with torch.cuda.stream(P.stream):
-        lam = torch.zeros((3, P.n), dtype=torch.float64, device=P.dev)
+        gen = torch.Generator(device=P.dev)
+        gen.manual_seed(0)
+        lam = torch.randn((3, P.n), dtype=torch.float64, device=P.dev, generator=gen)
         out = torch.zeros_like(lam)
         bbar = torch.zeros(P.n, dtype=torch.float64, device=P.dev)
         P.free = list(range(P.snapshots))

@@ -1058,8 +1058,14 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
                 gR[2] = lenR * mR[2];
             }
             Grad4 oL{0.0, 0.0, 0.0, 0.0}, oR{0.0, 0.0, 0.0, 0.0};
-            edge_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR,
-                             (int)((meta >> 15) & 3u));
+            // The VJP is linear in the cotangents of the edge's updates: where they are
+            // all zero (no gauge's cotangent has reached either cell yet) its outputs
+            // are zeros, and the edge needs no evaluation.
+            const long long gz = (dbits(gL[0]) | dbits(gL[1]) | dbits(gL[2]) | dbits(gR[0]) | dbits(gR[1]) |
+                                  dbits(gR[2])) << 1;
+            if (gz != 0)
+                edge_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, P.drytol, gL, gR, oL, oR,
+                                 (int)((meta >> 15) & 3u));
             if (bnd) {  // the ghost's cotangent goes back to the cell
                 if (P.bc == BC_SLIP) boundary_ghost_vjp<BC_SLIP>(n1, n2, oR, oL);
                 else if (P.bc == BC_NOSLIP) boundary_ghost_vjp<BC_NOSLIP>(n1, n2, oR, oL);
