@@ -927,8 +927,17 @@ __device__ __forceinline__ void edge_vjp(double n1, double n2, const State& QL, 
         lf_vjp<SOLVER>(n1, n2, QL, QR, dL, dR, drytol, gL, gR, oL, oR);
 }
 
+// Launch bounds of the reverse kernel: at most 256 threads; with SWE_ADJ_MIN_BLOCKS
+// defined, also that many resident CTAs of 256 threads (registers capped at
+// 65536 / (256 * SWE_ADJ_MIN_BLOCKS)). Undefined: the compiler's own register choice.
+#ifdef SWE_ADJ_MIN_BLOCKS
+#define SWE_ADJ_BOUNDS __launch_bounds__(256, SWE_ADJ_MIN_BLOCKS)
+#else
+#define SWE_ADJ_BOUNDS __launch_bounds__(256)
+#endif
+
 template <int SOLVER>
-__global__ void __launch_bounds__(256) adjoint_kernel(const AdjointArgs A) {
+__global__ void SWE_ADJ_BOUNDS adjoint_kernel(const AdjointArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int T = A.seg_cells;
     double* sh_h = reinterpret_cast<double*>(smem_raw);
