@@ -204,6 +204,31 @@ __device__ __forceinline__ void flush_instance(const StepArgs& A, int inst, doub
 // The edges between two segments, one thread each, before the step kernel:
 // the same flux as the step kernel's edge tasks (orientation by the step's
 // parity, pre-update states), both sides' updates stored by cell (a, then b).
+// depth_terms for the cross-edge pass: sqrt(g d) from the memo when the depth has
+// the same bits (the pass only reads it; the step kernel's owner CTAs write it),
+// and, for the f-wave, no RN(1 / d) for a cell with both momenta +-0 (its
+// quotients are zeros with the numerator's sign for any positive reciprocal).
+template <int SOLVER>
+__device__ __forceinline__ void cross_depth_terms(const StepArgs& A, int c, const State& Q, double drytol, double& d,
+                                                  double& sq, double& y) {
+    d = Q.h - Q.b;
+    const bool wet = lt(drytol, d);
+    sq = 0.0;
+    y = 0.0;
+    if (!wet) return;
+    bool hit = false;
+    if (A.memo) {
+        const double2 m = A.memo[c];
+        if (dbits(m.x) == dbits(d)) {
+            sq = m.y;
+            hit = true;
+        }
+    }
+    if (!hit) sq = sqrt(kG * d);
+    const bool still = ((dbits(Q.p1) | dbits(Q.p2)) << 1) == 0;
+    y = (SOLVER == FWAVE && still) ? 1.0 : recip_rn(d).y;
+}
+
 template <int SOLVER, int FZ = 0>
 __global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -234,8 +259,8 @@ __global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
     const State QL{hin[L], huin[L], hvin[L], A.b[L]};
     const State QR{hin[R], huin[R], hvin[R], A.b[R]};
     double dL, dR, sqL, sqR, yL, yR;
-    depth_terms(QL, drytol, dL, sqL, yL);
-    depth_terms(QR, drytol, dR, sqR, yR);
+    cross_depth_terms<SOLVER>(A, L, QL, drytol, dL, sqL, yL);
+    cross_depth_terms<SOLVER>(A, R, QR, drytol, dR, sqR, yR);
     Update fL, fR;
     edge_flux<SOLVER, FZ>(n1, n2, QL, QR, dL, dR, sqL, sqR, yL, yR, drytol, fL, fR, (int)((meta >> 15) & 3u),
                           FZ ? &A.xrec[j] : nullptr);
