@@ -379,13 +379,6 @@ int swe_step_host(swe_ctx* ctx, const double* h, const double* hu, const double*
  * No counterpart in the reference (the Fortran step divides directly). */
 int swe_division_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t* mismatches);
 
-/* Device self-check of the step's integer-pipe multiply (the products of the
- * f-wave path and the cell update): on n seeded random pairs with exponents in
- * [-exponent_span, exponent_span], plus zeros, subnormals, infinities and NaNs,
- * counts the products that differ from the FP64 multiply in any bit.
- * No counterpart in the reference. */
-int swe_multiply_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t* mismatches);
-
 /* Test-only device fault injection, off by default. No counterpart in the
  * reference (it has no bounded waits: it asserts). SWE_INJECT_STAGING_TX: the
  * step kernel arms each staging mbarrier for 16 bytes more than its bulk copies

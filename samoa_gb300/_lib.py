@@ -24,7 +24,7 @@ EXPORTS = [
     "swe_sample_gauges", "swe_adjoint_step", "swe_set_arith", "swe_traverse_branches", "swe_step_back",
     "swe_division_check", "swe_step_host", "swe_gauge_gradient",
     "swe_traverse_gauges", "swe_mesh_uniform_vertices", "swe_mesh_build", "swe_mesh_adapt",
-    "swe_multiply_check", "swe_set_staging", "swe_get_task_counts", "swe_set_cross_pass", "swe_traverse_frozen",
+    "swe_set_staging", "swe_get_task_counts", "swe_set_cross_pass", "swe_traverse_frozen",
     "swe_set_segment_order", "swe_set_fault_injection",
 ]
 
@@ -101,7 +101,6 @@ def load():
         "swe_traverse_gauges": [P, i64, i64, P, P],
         "swe_mesh_uniform_vertices": [i32, P],
         "swe_mesh_build": [i64, P, P, P, P, P, P, P, P, P, P],
-        "swe_multiply_check": [i64, C.c_uint64, i32, P],
         "swe_set_staging": [P, i32],
         "swe_mesh_adapt": [i64, P, P, P, P, P, P, i64, P, P, P, P, P, P, P],
     }

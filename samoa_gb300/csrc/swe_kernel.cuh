@@ -571,18 +571,18 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             double dh = 0.0, dp1 = 0.0, dp2 = 0.0, ds = 0.0;
             if (__any_sync(__activemask(), !quiet)) {
                 if (!quiet) {
-                    dh = z0(imul_cell(leg, u[0][0])) + imul_cell(hyp, u[0][1]);
-                    dh = dh + imul_cell(leg, u[0][2]);
-                    dp1 = z0(imul_cell(leg, u[1][0])) + imul_cell(hyp, u[1][1]);
-                    dp1 = dp1 + imul_cell(leg, u[1][2]);
-                    dp2 = z0(imul_cell(leg, u[2][0])) + imul_cell(hyp, u[2][1]);
-                    dp2 = dp2 + imul_cell(leg, u[2][2]);
+                    dh = z0(prod_cell(leg, u[0][0])) + prod_cell(hyp, u[0][1]);
+                    dh = dh + prod_cell(leg, u[0][2]);
+                    dp1 = z0(prod_cell(leg, u[1][0])) + prod_cell(hyp, u[1][1]);
+                    dp1 = dp1 + prod_cell(leg, u[1][2]);
+                    dp2 = z0(prod_cell(leg, u[2][0])) + prod_cell(hyp, u[2][1]);
+                    dp2 = dp2 + prod_cell(leg, u[2][2]);
                 }
             }
             if (__any_sync(__activemask(), sz != 0)) {
                 if (sz != 0) {
-                    ds = z0(imul_cell(leg, u[3][0])) + imul_cell(hyp, u[3][1]);
-                    ds = ds + imul_cell(leg, u[3][2]);
+                    ds = z0(prod_cell(leg, u[3][0])) + prod_cell(hyp, u[3][1]);
+                    ds = ds + prod_cell(leg, u[3][2]);
                 }
             }
             int8_t f = 0;
@@ -604,9 +604,9 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             if (quiet) {
                 dh = dp1 = dp2 = bitsd(dbits(ndv) & (long long)0x8000000000000000ULL);  // RN(ndv * +0)
             } else {
-                dh = imul_cell(ndv, dh);
-                dp1 = imul_cell(ndv, dp1);
-                dp2 = imul_cell(ndv, dp2);
+                dh = prod_cell(ndv, dh);
+                dp1 = prod_cell(ndv, dp1);
+                dp2 = prod_cell(ndv, dp2);
             }
             double h = sh_h[i], p1 = sh_hu[i], p2 = sh_hv[i];
             const double b = sh_b[i];

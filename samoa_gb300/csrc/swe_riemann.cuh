@@ -14,26 +14,6 @@
 #ifndef SWE_KNS
 #define SWE_KNS swe
 #endif
-// Which products run on the integer pipe (imul) instead of the FP64 pipe: the
-// solver's (delphi, Roe velocity, f-wave coefficients, quotients), the edge
-// rotations' and the cell update's. Off by default: measured on GB300 (2^26-cell
-// basin, autotuned tiling) the step ran at 2.40e9 cell-updates/s with all
-// products on the FP64 pipe, 2.35e9 with the cell update's on the integer pipe,
-// 2.24e9 with the rotations' or the solver's, 1.99e9 with all of them: the
-// integer multiply's ~30-instruction dependency chains stall the 12-16 warps
-// an SM holds at this register count more than the FP64 pipe's queue does.
-#ifndef SWE_IMUL
-#define SWE_IMUL 0
-#endif
-#ifndef SWE_IMUL_SOLVER
-#define SWE_IMUL_SOLVER SWE_IMUL
-#endif
-#ifndef SWE_IMUL_ROT
-#define SWE_IMUL_ROT SWE_IMUL
-#endif
-#ifndef SWE_IMUL_CELL
-#define SWE_IMUL_CELL SWE_IMUL
-#endif
 namespace swe {}
 
 #include <stdint.h>
@@ -71,46 +51,12 @@ __device__ __forceinline__ double z0(double x) {
     long long v = dbits(x);
     return bitsd(v == (long long)0x8000000000000000ULL ? 0LL : v);
 }
-// RN(a * b) on the integer pipe. GB300 retires ~500 G FP64 instructions/s but
-// has a wide integer pipe that the step barely uses; this moves a product
-// there (see SWE_IMUL for what that measured). Normal (or zero) operands with a normal
-// result: the 53 x 53-bit significand product (128-bit, __umul64hi + low half),
-// normalised by at most one bit, rounded to nearest even from the guard bit and
-// a sticky OR of the bits below, exponent ea + eb - bias (+1 on a carry out of
-// the rounding). Subnormal, infinite and NaN operands and results out of the
-// normal range take the FP64 multiply, so every input gives the IEEE product
-// (compared with the FP64 multiply bit for bit on the device by
-// swe_division_check's companion test, swe_multiply_check).
-__device__ __forceinline__ double imul_int(double a, double b) {
-    const unsigned long long A = dbits(a), B = dbits(b);
-    const unsigned long long S = (A ^ B) & 0x8000000000000000ULL;
-    const int ea = (int)((A >> 52) & 0x7ff), eb = (int)((B >> 52) & 0x7ff);
-    const unsigned long long M = 0x000fffffffffffffULL;
-    const bool za = (A << 1) == 0, zb = (B << 1) == 0;
-    if (za || zb) {  // +-0 times a finite number: a signed zero
-        if ((za && eb != 0x7ff) || (zb && ea != 0x7ff)) return bitsd((long long)S);
-        return a * b;
-    }
-    if (ea == 0 || eb == 0 || ea == 0x7ff || eb == 0x7ff) return a * b;
-    const unsigned long long ma = (A & M) | (1ULL << 52), mb = (B & M) | (1ULL << 52);
-    const unsigned long long hi = __umul64hi(ma, mb), lo = ma * mb;
-    const int norm = (int)(hi >> 41) & 1;  // product in [2^105, 2^106)
-    const int sh = 52 + norm;
-    unsigned long long m = (hi << (64 - sh)) | (lo >> sh);
-    const unsigned long long g = (lo >> (sh - 1)) & 1ULL;
-    const bool sticky = (lo & ((1ULL << (sh - 1)) - 1ULL)) != 0;
-    m += (g && (sticky || (m & 1ULL))) ? 1ULL : 0ULL;
-    int e = ea + eb - 1023 + norm;
-    if (m >> 53) {
-        m >>= 1;
-        ++e;
-    }
-    if (e < 1 || e > 2046) return a * b;
-    return bitsd((long long)(S | ((unsigned long long)e << 52) | (m & M)));
-}
-__device__ __forceinline__ double imul(double a, double b) { return SWE_IMUL_SOLVER ? imul_int(a, b) : a * b; }
-__device__ __forceinline__ double imul_rot(double a, double b) { return SWE_IMUL_ROT ? imul_int(a, b) : a * b; }
-__device__ __forceinline__ double imul_cell(double a, double b) { return SWE_IMUL_CELL ? imul_int(a, b) : a * b; }
+// The step's products, named by where they are taken (the solver's, the edge
+// rotations', the cell update's): plain FP64 multiplies. Moving them to the
+// integer pipe was measured slower (see the design notes of the FP64 diet).
+__device__ __forceinline__ double prod(double a, double b) { return a * b; }
+__device__ __forceinline__ double prod_rot(double a, double b) { return a * b; }
+__device__ __forceinline__ double prod_cell(double a, double b) { return a * b; }
 
 __device__ __forceinline__ double dmn(double a, double b) { return (a < b) ? a : b; }
 __device__ __forceinline__ double dmx(double a, double b) { return (a > b) ? a : b; }
@@ -243,7 +189,7 @@ __device__ __forceinline__ double div_rn(double a, const Recip& r) {
     if (!r.fast) return a / r.b;
     if ((dbits(a) << 1) == 0) return a * r.y;  // +-0 with the IEEE sign
     if (!exp_in(a, -500, 500)) return a / r.b;
-    double q = imul(a, r.y);
+    double q = prod(a, r.y);
     double res = fma(-r.b, q, a);
     q = fma(res, r.y, q);
     res = fma(-r.b, q, a);
@@ -628,10 +574,10 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
         }
     }
     const double hsum = hR + hL;
-    const double ghalf_h = imul(g * 0.5, hsum);  // (0.5 * g) * (hR + hL): delphi, chat, the f-wave's deldelphi
-    double delphi = ((imul(huR - huL, uL + uR) - imul(imul(uL, uR), hR - hL)) +
-                     imul(imul(0.5 * g, ((bR + hR) - bL) - hL), hsum)) -
-                    imul(ghalf_h, bR - bL);
+    const double ghalf_h = prod(g * 0.5, hsum);  // (0.5 * g) * (hR + hL): delphi, chat, the f-wave's deldelphi
+    double delphi = ((prod(huR - huL, uL + uR) - prod(prod(uL, uR), hR - hL)) +
+                     prod(prod(0.5 * g, ((bR + hR) - bL) - hL), hsum)) -
+                    prod(ghalf_h, bR - bL);
     // sqrt(g * h) after the wet/dry fix-ups: a wet side keeps its depth, a dry one
     // has depth 0, and a wall mirrors the wet side's depth
     // a dry side has h = 0 <= drytol now, a wet one is unchanged, a wall mirrors the wet side
@@ -642,7 +588,7 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     double sR = uR + sqR;
     // one division with its own divisor: the IEEE division (correctly rounded, as
     // recip_rn + div_rn is) needs fewer FP64 instructions than a private reciprocal
-    double uhat = (imul(sqL, uL) + imul(sqR, uR)) / (sqR + sqL);
+    double uhat = (prod(sqL, uL) + prod(sqR, uR)) / (sqR + sqL);
     double chat = sqrt(ghalf_h);
     const double r1 = uhat - chat, r2 = uhat + chat;
     double sE1 = fzb<FZ>(fz, 7, lt(sL, r1)) ? sL : r1;  // imin(sL, r1)
@@ -658,16 +604,16 @@ __device__ __forceinline__ void geoclaw_solver(double hL, double hR, double huL,
     } else {
         double delhu = huR - huL;
         double delb = bR - bL;
-        double deldelphi = -imul(ghalf_h, delb);
+        double deldelphi = -prod(ghalf_h, delb);
         double dpd = delphi - deldelphi;
         const Recip rD = recip_rn(sE2 - sE1);
-        double beta1 = div_rn(imul(sE2, delhu) - dpd, rD);
-        double beta2 = div_rn(dpd - imul(sE1, delhu), rD);
+        double beta1 = div_rn(prod(sE2, delhu) - dpd, rD);
+        double beta2 = div_rn(dpd - prod(sE1, delhu), rD);
         sw[0] = sE1; sw[1] = scale_pow2(sE1 + sE2, -1, 0.5); sw[2] = sE2;
-        fw[0][0] = beta1; fw[1][0] = imul(beta1, sE1); fw[2][0] = imul(beta1, vL);
-        fw[0][2] = beta2; fw[1][2] = imul(beta2, sE2); fw[2][2] = imul(beta2, vR);
+        fw[0][0] = beta1; fw[1][0] = prod(beta1, sE1); fw[2][0] = prod(beta1, vL);
+        fw[0][2] = beta2; fw[1][2] = prod(beta2, sE2); fw[2][2] = prod(beta2, vR);
         fw[0][1] = 0.0; fw[1][1] = 0.0;
-        fw[2][1] = ((imul(huR, vR) - imul(huL, vL)) - fw[2][0]) - fw[2][2];
+        fw[2][1] = ((prod(huR, vR) - prod(huL, vL)) - fw[2][0]) - fw[2][2];
     }
     // eliminate ghost fluxes of a wall (multiplication by 0 keeps the sign of zero)
     auto zero_wave = [&](const int w) {
@@ -783,8 +729,8 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
     double pL1, pL2, pR1, pR2;
     if (diag) {
         // RN(n1 p1) = +-a1, RN(n2 p2) = +-a2, RN(-n2 p1) = -+a1, RN(n1 p2) = +-a2
-        const double aL1 = imul_rot(c, QL.p1), aL2 = imul_rot(c, QL.p2);
-        const double aR1 = imul_rot(c, QR.p1), aR2 = imul_rot(c, QR.p2);
+        const double aL1 = prod_rot(c, QL.p1), aL2 = prod_rot(c, QL.p2);
+        const double aR1 = prod_rot(c, QR.p1), aR2 = prod_rot(c, QR.p2);
         pL1 = z0(flip(aL1, g1)) + flip(aL2, g2);
         pL2 = z0(flip(aL1, !g2)) + flip(aL2, g1);
         pR1 = z0(flip(aR1, g1)) + flip(aR2, g2);
@@ -799,10 +745,10 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         }
     } else {
         // T = [[n1, n2], [-n2, n1]]; p_edge = T p
-        pL1 = z0(imul_rot(n1, QL.p1)) + imul_rot(n2, QL.p2);
-        pL2 = z0(imul_rot(-n2, QL.p1)) + imul_rot(n1, QL.p2);
-        pR1 = z0(imul_rot(n1, QR.p1)) + imul_rot(n2, QR.p2);
-        pR2 = z0(imul_rot(-n2, QR.p1)) + imul_rot(n1, QR.p2);
+        pL1 = z0(prod_rot(n1, QL.p1)) + prod_rot(n2, QL.p2);
+        pL2 = z0(prod_rot(-n2, QL.p1)) + prod_rot(n1, QL.p2);
+        pR1 = z0(prod_rot(n1, QR.p1)) + prod_rot(n2, QR.p2);
+        pR2 = z0(prod_rot(-n2, QR.p1)) + prod_rot(n1, QR.p2);
     }
     double netL[3], netR[3], ms;
     geoclaw_solver<SOLVER, FZ>(dL, dR, pL1, pR1, pL2, pR2, QL.b, QR.b, sqL, sqR, yL, yR, drytol, netL, netR, ms,
@@ -814,8 +760,8 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
     const bool nfin = is_finite(netL[1]) && is_finite(netL[2]) && is_finite(netR[1]) && is_finite(netR[2]);
     if (diag && nfin) {
         // RN(m1 n1) = +-b1, RN(m2 (-n2)) = -+b2, RN(m1 n2) = +-b1, RN(m2 n1) = +-b2
-        const double bL1 = imul_rot(netL[1], c), bL2 = imul_rot(netL[2], c);
-        const double bR1 = imul_rot(netR[1], c), bR2 = imul_rot(netR[2], c);
+        const double bL1 = prod_rot(netL[1], c), bL2 = prod_rot(netL[2], c);
+        const double bR1 = prod_rot(netR[1], c), bR2 = prod_rot(netR[2], c);
         fL.p1 = z0(flip(bL1, g1)) + flip(bL2, !g2);
         fL.p2 = z0(flip(bL1, g2)) + flip(bL2, g1);
         fR.p1 = z0(flip(bR1, g1)) + flip(bR2, !g2);
@@ -830,10 +776,10 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         }
     } else {
         // p = net(2:3) T
-        fL.p1 = z0(imul_rot(netL[1], n1)) + imul_rot(netL[2], -n2);
-        fL.p2 = z0(imul_rot(netL[1], n2)) + imul_rot(netL[2], n1);
-        fR.p1 = z0(imul_rot(netR[1], n1)) + imul_rot(netR[2], -n2);
-        fR.p2 = z0(imul_rot(netR[1], n2)) + imul_rot(netR[2], n1);
+        fL.p1 = z0(prod_rot(netL[1], n1)) + prod_rot(netL[2], -n2);
+        fL.p2 = z0(prod_rot(netL[1], n2)) + prod_rot(netL[2], n1);
+        fR.p1 = z0(prod_rot(netR[1], n1)) + prod_rot(netR[2], -n2);
+        fR.p2 = z0(prod_rot(netR[1], n2)) + prod_rot(netR[2], n1);
     }
 }
 

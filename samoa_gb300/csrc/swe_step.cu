@@ -100,25 +100,6 @@ __global__ void division_check_kernel(int64_t n, unsigned long long seed, int e_
     if (bad) atomicAdd(mismatches, bad);
 }
 
-// Compares imul_int(a, b) with the FP64 multiply bit for bit (a NaN matches any NaN)
-// on seeded pairs that include zeros, subnormals, infinities and NaNs.
-__global__ void multiply_check_kernel(int64_t n, unsigned long long seed, int e_span, unsigned long long* mismatches) {
-    unsigned long long bad = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned long long z = seed + 2ULL * (unsigned long long)i;
-        double a = draw_double(z, e_span), b = draw_double(z + 1, e_span);
-        const unsigned long long k = mix64(z ^ 0x3333333333333333ULL);
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
-        if ((k & 31) == 0) a = __longlong_as_double((long long)(bits & 0x800fffffffffffffULL));    // zero / subnormal
-        if ((k & 31) == 1) a = __longlong_as_double((long long)(bits | 0x7ff0000000000000ULL));    // inf / NaN
-        if ((k & 31) == 2) b = __longlong_as_double((long long)(k & 0x8000000000000000ULL));       // +-0
-        const double x = imul_int(a, b), y = a * b;
-        const bool ok = (x != x && y != y) || __double_as_longlong(x) == __double_as_longlong(y);
-        bad += ok ? 0 : 1;
-    }
-    if (bad) atomicAdd(mismatches, bad);
-}
-
 __global__ void set_times_kernel(InstScalars* S, const double* t, const double* dt, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         S[i].time = t[i];
@@ -1512,27 +1493,6 @@ int swe_division_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t*
     if (e == cudaSuccess) e = cudaMemcpy(&got, d, sizeof(got), cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return set_error(SWE_E_CUDA, "division check: %s", cudaGetErrorString(e));
-    *mismatches = (int64_t)got;
-    return SWE_OK;
-}
-
-int swe_multiply_check(int64_t n, uint64_t seed, int32_t exponent_span, int64_t* mismatches) {
-    if (n < 0 || !mismatches || exponent_span < 0 || exponent_span > 1022)
-        return set_error(SWE_E_INVALID, "bad arguments");
-    *mismatches = 0;
-    if (n == 0) return SWE_OK;
-    unsigned long long* d = nullptr;
-    int rc = device_alloc((void**)&d, sizeof(unsigned long long));
-    if (rc) return rc;
-    cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long));
-    if (e == cudaSuccess) {
-        multiply_check_kernel<<<1216, 256>>>(n, (unsigned long long)seed, exponent_span, d);
-        e = cudaGetLastError();
-    }
-    unsigned long long got = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&got, d, sizeof(got), cudaMemcpyDeviceToHost);
-    cudaFree(d);
-    if (e != cudaSuccess) return set_error(SWE_E_CUDA, "multiply check: %s", cudaGetErrorString(e));
     *mismatches = (int64_t)got;
     return SWE_OK;
 }

@@ -5,7 +5,6 @@
 #include <cuda_runtime.h>
 
 #define SWE_KNS swe_fma
-#define SWE_IMUL 0  // products stay on the FP64 pipe, where they fuse with the adds (also the default)
 #include "swe_kernel.cuh"
 
 namespace swe {

@@ -418,13 +418,3 @@ def test_division_with_shared_reciprocal_is_ieee(swe_lib, span):
     assert bad.value == 0
 
 
-@pytest.mark.parametrize("span", [30, 500, 1022])
-def test_integer_pipe_multiply_is_ieee(swe_lib, span):
-    """The step's products on the integer pipe equal the FP64 multiply bit for
-    bit: 2^25 seeded pairs per exponent span, with zeros, subnormals, infinities
-    and NaNs mixed in (those take the FP64 multiply)."""
-    import ctypes as C
-    from samoa_gb300 import _lib
-    bad = C.c_int64(-1)
-    _lib.check(swe_lib.swe_multiply_check(1 << 25, 4321 + span, span, C.byref(bad)))
-    assert bad.value == 0
