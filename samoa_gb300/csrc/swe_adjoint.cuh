@@ -955,6 +955,27 @@ __global__ void SWE_ADJ_BOUNDS adjoint_kernel(const AdjointArgs A) {
     for (int seg = blockIdx.x; seg < A.n_seg; seg += gridDim.x) {
         const int4 si = __ldg(&A.seg_info[seg]);
         const int c0 = si.x, cn = si.y;
+        if (tid == 0 && seg + (int)gridDim.x < A.n_seg) {
+            // this CTA's next segment (the deal is static) is on its way to L2
+            // while the CTA works on this one: its state, cotangents, bathymetry
+            // cotangent, memo entries, depths, branch records and edge tasks
+            const int nx = seg + (int)gridDim.x;
+            const int4 sn = __ldg(&A.seg_info[nx]);
+            const size_t bytes = (size_t)sn.y * 8u;
+            prefetch_l2(A.h + sn.x, bytes);
+            prefetch_l2(A.hu + sn.x, bytes);
+            prefetch_l2(A.hv + sn.x, bytes);
+            prefetch_l2(A.b + sn.x, bytes);
+            prefetch_l2(A.lam_h + sn.x, bytes);
+            prefetch_l2(A.lam_hu + sn.x, bytes);
+            prefetch_l2(A.lam_hv + sn.x, bytes);
+            prefetch_l2(A.bbar + sn.x, bytes);
+            if (A.memo) prefetch_l2(A.memo + sn.x, (size_t)sn.y * 16u);
+            prefetch_l2(A.depth + sn.x, (size_t)sn.y);
+            prefetch_l2(A.branch + sn.x, (size_t)sn.y);
+            const long long a = __ldg(&A.seg_ptr[nx]), e = __ldg(&A.seg_ptr[nx + 1]);
+            prefetch_l2(A.tasks + a, (size_t)(e - a) * 16u);
+        }
         for (int i = tid; i < cn; i += blockDim.x) {
             const int cc = c0 + i;
             const double h = A.h[cc], b = A.b[cc];

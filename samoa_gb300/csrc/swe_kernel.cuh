@@ -131,6 +131,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// Prefetch into L2 the 16-byte-aligned part of [p, p + bytes), for any p (the
+// bulk prefetch wants a 16-byte aligned address and size): it touches no byte
+// outside the range, writes nothing, and has no completion to wait for.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+    const uintptr_t a = ((uintptr_t)p + 15u) & ~(uintptr_t)15u, e = ((uintptr_t)p + bytes) & ~(uintptr_t)15u;
+    if (e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)));
+}
+
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
@@ -273,6 +282,43 @@ __global__ void __launch_bounds__(256) cross_edges_kernel(const StepArgs A) {
     out[3] = make_double2(ub.p2, ub.s);
 }
 
+// Round-up float of |x| for x = +-0 or 2^-100 <= |x| < 2^101, from the bit
+// pattern (integer operations): the significand truncated to 23 bits plus one
+// unit in the last place (a carry into the exponent is still an upper bound).
+// False for other x (tiny, huge, inf, NaN).
+__device__ __forceinline__ bool float_up(double x, float& f) {
+    const unsigned long long a = (unsigned long long)abs_bits(x);
+    f = 0.0f;
+    if (a == 0ull) return true;
+    const int e = (int)(a >> 52) - 1023;
+    if (e < -100 || e > 100) return false;
+    f = __uint_as_float(((unsigned)(e + 127) << 23 | (unsigned)((a >> 29) & 0x7fffffull)) + 1u);
+    return true;
+}
+
+// True when the CFL key RN(ds 2^k) of a cell is certainly below the key m (bits
+// of a nonnegative double), so that the cell cannot raise a maximum >= m; ds =
+// RN(RN(RN(leg s0) + RN(hyp s1)) + RN(leg s2)) is the cell update's speed sum,
+// up = (leg, hyp) rounded up to float. U = leg s0 + hyp s1 + leg s2 evaluated in
+// float with every operand and every operation rounded up bounds the exact sum
+// of the magnitudes S; the three roundings of ds give |ds| <= S (1 + 2^-53)^3
+// (and an absolute error below 2^-1072 where a result is subnormal), both below
+// the margin U 2^-20 of a normal float U; 2^k scales exactly, and a bound that
+// is not a finite double gives false. The float work runs beside the FP64 pipe.
+__device__ __forceinline__ bool key_below(float2 up, double s0, double s1, double s2, int k, unsigned long long m) {
+    float f0, f1, f2;
+    if (!float_up(s0, f0) || !float_up(s1, f1) || !float_up(s2, f2)) return false;
+    float U = __fmaf_ru(up.x, f0, __fmaf_ru(up.y, f1, __fmul_ru(up.x, f2)));
+    U = __fmul_ru(U, 1.00000095367431640625f);  // 1 + 2^-20
+    const unsigned int ub = __float_as_uint(U);
+    const int ef = (int)(ub >> 23);  // U >= 0
+    if (ef == 0 || ef == 255) return false;
+    const int eb = ef - 127 + 1023 + k;
+    if (eb >= 2047) return false;
+    const unsigned long long bound = ((unsigned long long)eb << 52) | ((unsigned long long)(ub & 0x7fffffu) << 29);
+    return bound < m;
+}
+
 template <int SOLVER, int FZ = 0>
 __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -289,6 +335,7 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
     double* tab_vol = tab_hyp + A.max_ndepth;
     double* tab_ndv = tab_vol + A.max_ndepth;  // -dt / volume
     double* tab_pow = tab_ndv + A.max_ndepth;  // 2^(d+1)
+    float2* tab_up = reinterpret_cast<float2*>(tab_pow + A.max_ndepth);  // (leg, hyp) rounded up to float
     __shared__ uint64_t bar[2];
     __shared__ double red_min[32];
     __shared__ unsigned long long red_max[32];
@@ -344,6 +391,14 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
                 bulk_g2s(bh + 3 * T, A.b + c0, bytes, &bar[k]);
             }
             pending |= 1u << k;
+        }
+        if (tid == 0) {
+            // the segment's edge tasks, memo entries and depths, read later in
+            // task or thread order, are on their way to L2 while its state lands
+            const long long a = __ldg(&A.seg_ptr[sg]), e = __ldg(&A.seg_ptr[sg + 1]);
+            prefetch_l2(A.tasks + a, (size_t)(e - a) * 16u);
+            if (A.memo) prefetch_l2(A.memo + c0, (size_t)cn * 16u);
+            prefetch_l2(A.depth + c0, (size_t)cn);
         }
         for (int i = cbulk + tid; i < cn; i += blockDim.x) {
             bh[i] = hin[c0 + i];
@@ -406,8 +461,10 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             for (int i = tid; i < P.ndepth; i += blockDim.x) {
                 const int d = P.dmin + i;
                 const double vol = (P.scaling * P.scaling) * c_vol[d];
-                tab_leg[i] = P.scaling * c_leg[d + 1];
-                tab_hyp[i] = P.scaling * c_leg[d];
+                const double leg = P.scaling * c_leg[d + 1], hyp = P.scaling * c_leg[d];
+                tab_leg[i] = leg;
+                tab_hyp[i] = hyp;
+                tab_up[i] = make_float2(__double2float_ru(leg), __double2float_ru(hyp));
                 tab_vol[i] = vol;
                 tab_ndv[i] = -dt / vol;
                 tab_pow[i] = ldexp(2.0, d);
@@ -479,8 +536,12 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         __syncthreads();
 
         // ---- 2. edge tasks (skeleton_scalar_op / bnd_skeleton_scalar_op, :196-255)
+        // each thread loads its next task while it works on the current one
+        int4 tk_next = make_int4(0, 0, 0, 0);
+        if (t0 + tid < tm) tk_next = __ldg(&A.tasks[t0 + tid]);
         for (long long t = t0 + tid; t < tm; t += blockDim.x) {
-            const int4 tk = __ldg(&A.tasks[t]);
+            const int4 tk = tk_next;
+            if (t + blockDim.x < tm) tk_next = __ldg(&A.tasks[t + blockDim.x]);
             const uint32_t meta = (uint32_t)tk.z;
             const bool bnd = (meta >> 14) & 1u;
             int L, R, iL, iR, pL;
@@ -547,6 +608,9 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
 
         // ---- 3. cell updates: cell_update_op + volume_op (src/SWE/SWE_euler_timestep.f90:257-355)
         const int k0 = odd ? 2 : 0, k2 = odd ? 0 : 2;
+        // the largest CFL key the lanes of this warp have taken so far (dt_by_max);
+        // a cell whose key is certainly below it cannot raise the maximum
+        const unsigned long long wkey = P.dt_by_max ? warp_max_u64(dskey) : 0ull;
         for (int i = tid; i < cn; i += blockDim.x) {
             const int c = c0 + i;
             const int d = A.depth[c];
@@ -564,9 +628,8 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             // quiet: every update of h, hu, hv is +-0 (dry land, water at rest). Then
             // each sum below is +0 (positive edge lengths), RN(ndv * +0) is a zero with
             // ndv's sign, and adding it leaves the state as add_zero says: the same
-            // bits, without the FP64 arithmetic. The speed sum ds is +0 when every
-            // speed is +-0 (dry land), else it is summed (water at rest still has
-            // wave speeds).
+            // bits, without the FP64 arithmetic. Water at rest still has wave speeds,
+            // so the speed sum ds has its own test below.
             const bool quiet = nz == 0 && is_finite(ndv);
             double dh = 0.0, dp1 = 0.0, dp2 = 0.0, ds = 0.0;
             if (__any_sync(__activemask(), !quiet)) {
@@ -579,8 +642,12 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
                     dp2 = dp2 + prod_cell(leg, u[2][2]);
                 }
             }
-            if (__any_sync(__activemask(), sz != 0)) {
-                if (sz != 0) {
+            // ds is +0 when every speed is +-0 (dry land) or when the cell's key stays
+            // below wkey (key_below), else it is summed
+            bool need_ds = sz != 0;
+            if (need_ds && wkey != 0ull) need_ds = !key_below(tab_up[di], u[3][0], u[3][1], u[3][2], d + 1, wkey);
+            if (__any_sync(__activemask(), need_ds)) {
+                if (need_ds) {
                     ds = z0(prod_cell(leg, u[3][0])) + prod_cell(hyp, u[3][1]);
                     ds = ds + prod_cell(leg, u[3][2]);
                 }

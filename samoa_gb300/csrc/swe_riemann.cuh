@@ -708,10 +708,15 @@ __device__ __forceinline__ void geoclaw_flux(double n1, double n2, const State& 
         // are monotone), hence chat <= RN(sqrt(RN(g h))), the cell's own
         // sqrt(g h). So the maximum speed is max(sqL, sqR), both positive. The
         // same bits as the full evaluation, without its FP64 arithmetic.
+        // The surface difference x - hL, x = RN(RN(bR + hR) - bL), rounds to a
+        // zero exactly when x equals hL and both are finite (gradual underflow:
+        // the difference of two distinct finite doubles is not rounded to zero;
+        // inf - inf is NaN). hL > drytol >= 0 is positive, so equal values have
+        // equal bit patterns: one FP64 addition fewer per edge.
         const bool still = ((dbits(QL.p1) | dbits(QL.p2) | dbits(QR.p1) | dbits(QR.p2)) << 1) == 0;
         if (still && lt(drytol, dL) && lt(drytol, dR)) {
-            const double surf = ((QR.b + dR) - QL.b) - dL;
-            if ((dbits(surf) << 1) == 0) {
+            const double x = (QR.b + dR) - QL.b;
+            if (dbits(x) == dbits(dL) && is_finite(dL)) {
                 const long long m = dbits(sqL) > dbits(sqR) ? dbits(sqL) : dbits(sqR);
                 const double ms = bitsd(m);
                 fL = Update{0.0, 0.0, 0.0, ms};

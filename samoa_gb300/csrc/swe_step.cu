@@ -346,8 +346,8 @@ int device_alloc(void** p, size_t bytes) {
 }
 
 size_t smem_bytes_for(int64_t seg_cells, int stage_depth, int max_ndepth) {
-    // staging [depth][4][T], RN(1/depth) and sqrt(g depth) [2][T], edge slots [12][T], depth tables [5][nd]
-    return (size_t)(14 + 4 * stage_depth) * (size_t)seg_cells * sizeof(double) + (size_t)5 * max_ndepth * sizeof(double);
+    // staging [depth][4][T], RN(1/depth) and sqrt(g depth) [2][T], edge slots [12][T], depth tables [6][nd]
+    return (size_t)(14 + 4 * stage_depth) * (size_t)seg_cells * sizeof(double) + (size_t)6 * max_ndepth * sizeof(double);
 }
 
 size_t smem_bytes(const swe_ctx* c) { return smem_bytes_for(c->seg_cells, c->stage_depth, c->max_ndepth); }
