@@ -1,7 +1,7 @@
 """ctypes front end of the oracle (test infrastructure only).
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
-may import this module, and only as the checker. It wraps ``swe_oracle.c``, the
+may import this module, and only as the reference results are compared with. It wraps ``swe_oracle.c``, the
 strict-IEEE C restatement of sam(oa)^2's SWE Euler step, and ``swe_oracle_adapt.c``,
 the restatement of one adaption step and of the integrated bathymetry.
 """

@@ -3,7 +3,7 @@
  *
  * A plain-C, strict-IEEE (no FMA contraction, no fast-math) restatement of the
  * sam(oa)^2 shallow-water (SWE) explicit Euler time step, used by tests/, by
- * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg, as the reference that results are compared with.
  *
  * What it restates (paths are relative to the meistero/Samoa source tree):
  *   - Sierpinski mesh generation and cell types ........ src/SFC_node_traversal.f90:85-292,

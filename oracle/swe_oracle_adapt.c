@@ -3,7 +3,7 @@
  *
  * A plain-C restatement of one adaption step of sam(oa)^2's SWE scenario (the
  * remesh between two time steps) and of its bathymetry sampling, used by tests/
- * as the checker of the product's host adaptivity. What it restates (paths
+ * as the reference the product's host adaptivity is compared with. What it restates (paths
  * relative to the meistero/Samoa source tree):
  *   - the conformity traversal: edge flags refine (initially false), coarsen
  *     (initially true) and remove, set per cell by mark_edges and
