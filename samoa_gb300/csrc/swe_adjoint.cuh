@@ -417,21 +417,44 @@ __device__ __forceinline__ void geoclaw_vjp(double n1, double n2, const State& Q
         // beta1 (1, sE1 n) (sE1 < 0), the right one beta2 (1, sE2 n) (sE2 > 0);
         // the middle wave's components are products of two zeros.
         const bool still = ((dbits(QL.p1) | dbits(QL.p2) | dbits(QR.p1) | dbits(QR.p2)) << 1) == 0;
-        if (still && lt(drytol, dL0) && lt(drytol, dR0) && (dbits(((QR.b + dR0) - QL.b) - dL0) << 1) == 0) {
+        // (the surface difference x - dL0 is a zero exactly when x = RN(RN(bR + dR0) - bL) equals dL0 > 0 and
+        // both are finite, as in the forward step's test)
+        if (still && lt(drytol, dL0) && lt(drytol, dR0) && dbits((QR.b + dR0) - QL.b) == dbits(dL0) &&
+            is_finite(dL0)) {
             const double ghalf = c * (dR0 + dL0);
             const double chat = sqrt(ghalf);
             const double sE1 = -imax(sqL0, chat), sE2 = imax(sqR0, chat);
             const double rD = rcp_nr(sE2 - sE1);
-            const double gb1 = gL[0] + sE1 * (n1 * gL[1] + n2 * gL[2]);
-            const double gb2 = gR[0] + sE2 * (n1 * gR[1] + n2 * gR[2]);
-            const double g_du = (sE2 * gb1 - sE1 * gb2) * rD;  // cotangent of delhu
-            const double g_dh = ghalf * ((gb2 - gb1) * rD);    // of hR' (minus it for hL')
+            // n . (g1, g2) of each side's cotangent: a signed component for the
+            // axis-aligned normals (1, 0) and (0, 1) up to sign, whose other
+            // component is a zero; the cotangents need no bit-exact rounding, so
+            // products are fused
+            const bool ax = axis != 0;
+            const int k = axis == 2 ? 2 : 1;
+            const bool sg = axis == 2 ? lt0(n2) : lt0(n1);
+            const double nL = ax ? flip(gL[k], sg) : fma(n1, gL[1], n2 * gL[2]);
+            const double nR = ax ? flip(gR[k], sg) : fma(n1, gR[1], n2 * gR[2]);
+            const double gb1 = fma(sE1, nL, gL[0]);
+            const double gb2 = fma(sE2, nR, gR[0]);
+            const double g_du = fma(sE2, gb1, -(sE1 * gb2)) * rD;  // cotangent of delhu
+            const double g_dh = ghalf * ((gb2 - gb1) * rD);          // of hR' (minus it for hL')
             outL.h -= g_dh;
             outR.h += g_dh;
-            outL.hu -= g_du * n1;
-            outL.hv -= g_du * n2;
-            outR.hu += g_du * n1;
-            outR.hv += g_du * n2;
+            if (ax) {
+                const double t = flip(g_du, sg);
+                if (k == 1) {
+                    outL.hu -= t;
+                    outR.hu += t;
+                } else {
+                    outL.hv -= t;
+                    outR.hv += t;
+                }
+            } else {
+                outL.hu = fma(-g_du, n1, outL.hu);
+                outL.hv = fma(-g_du, n2, outL.hv);
+                outR.hu = fma(g_du, n1, outR.hu);
+                outR.hv = fma(g_du, n2, outR.hv);
+            }
             return;
         }
     }
