@@ -607,6 +607,10 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
         __syncthreads();
 
         // ---- 3. cell updates: cell_update_op + volume_op (src/SWE/SWE_euler_timestep.f90:257-355)
+        // With one staging buffer, thread 0 takes the next segment's ticket now and
+        // reads it after its cells, so the atomic's round trip overlaps the updates.
+        unsigned int ticket = 0u;
+        if (!depth2 && tid == 0) ticket = atomicAdd(&A.gs->next_seg, 1u);
         const int k0 = odd ? 2 : 0, k2 = odd ? 0 : 2;
         // the largest CFL key the lanes of this warp have taken so far (dt_by_max);
         // a cell whose key is certainly below it cannot raise the maximum
@@ -708,10 +712,12 @@ __global__ void SWE_STEP_BOUNDS step_kernel(const StepArgs A) {
             hvout[c] = p2;
             A.flags[c] = f;
         }
+        if (!depth2 && tid == 0) {
+            const int k = (int)ticket;
+            s_seg = k < A.n_seg ? (A.seg_order ? __ldg(&A.seg_order[k]) : k) : A.n_seg;
+        }
         __syncthreads();
-        if (!depth2) {  // draw and stage the next segment now
-            if (tid == 0) draw();
-            __syncthreads();
+        if (!depth2) {  // stage the next segment now
             seg_next = s_seg;
             if (seg_next < A.n_seg) issue(seg_next, 0);
         } else {
