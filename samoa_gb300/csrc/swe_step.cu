@@ -725,10 +725,13 @@ int launch_steps(swe_ctx* c, int64_t n_steps, uint8_t* branch = nullptr, double*
         k = (void*)step_kernel<FWAVE, 2>;
         kx = (void*)cross_edges_kernel<FWAVE, 2>;
     }
-    const unsigned xblocks = pass ? (unsigned)((c->n_xtasks + 255) / 256) : 0u;
+    // the cross-edge pass waits mostly on its scattered cell reads: 128-thread CTAs
+    // (90 registers) fit 5 per SM, 20 warps, against 2 CTAs of 256 threads
+    constexpr int kCrossThreads = 128;
+    const unsigned xblocks = pass ? (unsigned)((c->n_xtasks + kCrossThreads - 1) / kCrossThreads) : 0u;
     void* args[] = {&A};
     for (int64_t s = 0; s < n_steps; ++s) {
-        if (xblocks) CUDA_TRY(cudaLaunchKernel(kx, dim3(xblocks), dim3(256), args, 0, c->stream));
+        if (xblocks) CUDA_TRY(cudaLaunchKernel(kx, dim3(xblocks), dim3(kCrossThreads), args, 0, c->stream));
         CUDA_TRY(cudaLaunchKernel(k, dim3(c->grid), dim3(c->block_threads), args, c->smem, c->stream));
         if (!c->capturing) ++c->step_mirror;
     }
