@@ -275,6 +275,50 @@ def test_mass_conservation_and_drift(swe_lib, oracle_lib):
         trav.close()
 
 
+@pytest.mark.parametrize("huge", [False, True])
+@pytest.mark.parametrize("tiling", [(64, 64), (384, 128)])
+def test_cfl_bound_near_ties(swe_lib, oracle_lib, tiling, huge):
+    """The cell update skips a cell's CFL speed sum when a float upper bound of
+    its key stays below the largest key its warp has taken (key_below): dt_new
+    must still be the maximum over every cell, bit for bit with the oracle.
+    A lake at rest over random depths 10..15 m (so most cells are skipped once
+    a warp has met a deep one), whose deepest depth recurs at scattered cells
+    and, 2e-12 relative deeper (far inside the bound's 2^-20 margin), at one
+    cell near the end of the curve; with `huge`, one cell 1e60 m deep, whose
+    speed (~3e30) lies outside the range the bound handles. 2^18 cells in
+    64- or 384-cell segments: several segments per CTA, so warps carry a
+    running maximum from segment to segment."""
+    d = 18
+    mesh = swe.uniform_mesh(d)
+    n = mesh.n_cells
+    rng = np.random.default_rng(77)
+    b = -(10.0 + 5.0 * rng.random(n))
+    m = int(np.argmin(b))
+    ties = rng.choice(n, 64, replace=False)
+    b[ties] = b[m]
+    b[n - 1 - int(rng.integers(0, 1000))] = b[m] * (1.0 + 2e-12)
+    if huge:
+        b[int(rng.integers(n // 2, n))] = -1e60
+    h = np.zeros(n)
+    cfg = swe.Config(flux_solver="fwave", boundary="outflow", courant_number=0.45, dry_tolerance=1e-3,
+                     scaling=1.0, offset=(-0.5, -0.5), i_min_depth=d - 1, i_max_depth=d + 1)
+    g = swe.Grid(mesh, h, np.zeros(n), np.zeros(n), b, 0.0, 1e-6)
+    S = omp_state(mesh, g)
+    P = oracle_params(cfg)
+    trav = swe.SweEulerTimestepTraversal(cfg)
+    trav.set_tiling(*tiling)
+    try:
+        for k in range(3):
+            trav.traverse(g)
+            S.steps(P, 1)
+            tag = "near ties %s step %d" % (tiling, k)
+            assert_state_equal(tag, g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+            assert g.r_dt_new == S.dt_new, (tag, g.r_dt_new, S.dt_new)
+            assert g.r_time == S.scal[0] and g.r_dt == S.scal[1], tag
+    finally:
+        trav.close()
+
+
 def test_determinism(swe_lib):
     out = []
     for _ in range(2):
