@@ -148,22 +148,26 @@ def _odd_mesh(depth):
 
 
 def test_full_size_basin_against_omp(swe_lib, oracle_lib):
-    """The bench workload itself, 2^26 cells with the autotuned tiling (512 x 128)
-    and the cross-edge pass: three steps bit-exact against the OpenMP oracle,
-    state, flags, dt."""
-    scn = scenarios.ocean_basin(log2_cells=26, steps=3, device="cuda")
+    """The bench workload itself, 2^26 cells with the autotuned tiling (384 x 128)
+    and the cross-edge pass: 20 steps bit-exact against the OpenMP oracle, state,
+    flags and dt compared after steps 1, 2, 3, 10 and 20 (time and dt carry every
+    step's CFL maximum, so a step in between that differed would show)."""
+    scn = scenarios.ocean_basin(log2_cells=26, steps=20, device="cuda")
     g = scn.grid
     S = omp_state(g.mesh, g)
     P = oracle_params(scn.cfg)
     trav = swe.SweEulerTimestepTraversal(scn.cfg)
-    trav.set_tiling(512, 128)
+    trav.set_tiling(384, 128)
     try:
-        for k in range(3):
-            S.steps(P, 1)
-            trav.traverse(g)
-            assert_state_equal("2^26 basin step %d" % k, g.h, g.hu, g.hv, S.h, S.hu, S.hv)
+        done = 0
+        for k in (1, 1, 1, 7, 10):
+            S.steps(P, k)
+            trav.traverse(g, steps=k)
+            done += k
+            assert_state_equal("2^26 basin after %d steps" % done, g.h, g.hu, g.hv, S.h, S.hu, S.hv)
             assert np.array_equal(g.refinement, S.flags)
             assert g.r_dt == S.scal[1] and g.r_time == S.scal[0]
+            assert g.r_dt_new == S.dt_new
     finally:
         trav.close()
 
