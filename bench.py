@@ -514,6 +514,7 @@ def adjoint_compare(a, device):
         t_step, t_adj = adjoint.time_steps(P, case["h0"], case["b"], 50)
     finally:
         P.close()
+    all_states = adjoint_all_states(a, case, device, t_fwd, J)
     windowed = adjoint_windowed(a, case, device)
     try:
         moving_fd = adjoint_moving_fd(device)
@@ -532,7 +533,7 @@ def adjoint_compare(a, device):
             "fd_frozen_rel_err_b_along_gradient": fb, "fd_frozen_directions_b": len(fbr),
             "fd_frozen_max_err_over_grad_norm_b": max(fbr, default=None),
             "forward_step_ms": 1e3 * t_step, "adjoint_step_ms": 1e3 * t_adj, "adjoint_step_over_forward_step": t_adj / t_step,
-            "windowed": windowed, "fd_moving_water": moving_fd,
+            "windowed": windowed, "all_states": all_states, "fd_moving_water": moving_fd,
             "note": "gradient_s = one checkpointed sweep (its first descent is the forward run; recomputation "
                     "included); J(h0, b) is the squared misfit at 32 gauges; dt frozen, FD with the same dts, "
                     "eps = 1e-6 relative, seeded N(0,1) directions on the cells deeper than 100 m. J is piecewise "
@@ -546,6 +547,28 @@ def adjoint_compare(a, device):
                     "|g| |d|: the shelf is flat, so many directional derivatives are tiny). Perturbing b "
                     "reorders neighbouring depths at rest and so crosses the Einfeldt min/max kinks over 2,000 "
                     "steps, so plain FD in b is kink-limited"}
+
+
+def adjoint_all_states(a, case, device, t_fwd, J):
+    """The same gradient with a slot for every step's state (2,000 x 24 B x 2^18
+    cells = 12.6 GB of HBM) instead of the configuration's 64: the first descent
+    stores every state and no step is recomputed, which separates the cost of
+    the 64-slot budget from the cost of the reverse steps themselves."""
+    from samoa_gb300 import adjoint
+    P = adjoint.GaugeProblem(case["mesh"], case["params"], case["gauges"], case["obs"], case["dts"],
+                             snapshots=a.adjoint_steps, device=device)
+    try:
+        P.gradient(case["h0"], case["b"])  # warm-up
+        P.stats = {"forward_steps": 0, "adjoint_steps": 0}
+        t0 = time.perf_counter()
+        Jg, _, _ = P.gradient(case["h0"], case["b"])
+        t_grad = time.perf_counter() - t0
+        stats = dict(P.stats)
+    finally:
+        P.close()
+    return {"snapshots": a.adjoint_steps, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+            "forward_steps_in_gradient": stats["forward_steps"], "J_rel_diff": abs(Jg - J) / abs(J),
+            "note": "not the configuration (64 stored states): every state kept, no recomputation"}
 
 
 def adjoint_moving_fd(device, steps=100, n_dir=6):
