@@ -145,3 +145,20 @@ def test_the_check_catches_a_bound_rounded_to_nearest():
         b = _bits(float(u * 2 ** 10))
         bad += key_bits(leg, hyp, s, 10) > b
     assert bad > 0
+
+
+def test_division_free_cfl_reduction_equals_the_per_cell_minimum():
+    """The kernel's CFL reduction: with volume(d) = V 2^-(d+1) exactly (V =
+    RN(scaling^2)), min over cells of RN(volume(d) / ds) equals
+    RN(V / max over cells of ds 2^(d+1)), since RN(V / x) is monotone in x and
+    the power-of-two scalings are exact (volumes and keys normal numbers)."""
+    rng = np.random.default_rng(3)
+    for _ in range(3000):
+        scaling = float(2.0 ** rng.uniform(-5, 25))
+        V = scaling * scaling
+        n = int(rng.integers(1, 64))
+        depths = rng.integers(0, 40, n)
+        ds = [float(2.0 ** rng.uniform(-30, 30)) * (1 + float(rng.random())) for _ in range(n)]
+        ref = min(math.ldexp(V, -(int(d) + 1)) / x for d, x in zip(depths, ds))
+        keys = [math.ldexp(x, int(d) + 1) for d, x in zip(depths, ds)]
+        assert V / max(keys) == ref
