@@ -258,7 +258,8 @@ def fp64_dgemm_tflops(torch):
 
 
 ENSEMBLE_TILINGS = [(256, 128), (384, 128), (512, 128), (512, 256)]
-E2E_TILINGS = [(384, 128, 1), (384, 128, 2), (256, 128, 2), (512, 128, 2), (512, 256, 2), (768, 256, 1)]
+E2E_TILINGS = [(384, 128, 1), (384, 128, 2), (256, 128, 2), (512, 128, 2), (512, 256, 1), (512, 256, 2),
+               (640, 256, 1), (768, 256, 1)]
 
 
 def _time_batched(meshes, grids, cfgs, K, stream, device, tiling=None):
