@@ -141,7 +141,7 @@ int swe_last_error(char* buf, size_t n);
  * per block (multiple of 32, 64..256); 0 keeps
  * the current value. A mesh upload or
  * this call rebuilds the segment task lists. Until a segment length is set
- * here, each mesh upload picks it by size: 512 cells from 2^20 cells on, 256
+ * here, each mesh upload picks it by size: 384 cells from 2^20 cells on, 256
  * below (more segments than resident CTAs on small meshes). */
 int swe_set_tiling(swe_ctx* ctx, int32_t segment_cells, int32_t block_threads);
 

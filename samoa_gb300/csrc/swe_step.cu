@@ -243,12 +243,14 @@ struct swe_ctx {
     int64_t cells_packed = 0;      // sum of the instances' cells (host layout)
     bool has_mesh = false, has_state = false;
     // tiling
-    // 512 x 128: the best of a sweep on GB300 (2^22..2^26 cells). Until the caller
-    // sets a tiling, meshes below 2^20 cells get 256-cell segments: with 512 a
-    // 2^18-cell mesh has 512 segments for ~456 resident CTAs, and a step takes
-    // two segment-times (measured at 2^18: forward step 0.170 -> 0.145 ms,
-    // adjoint step 0.242 -> 0.222 ms).
-    int32_t seg_cells = 512, block_threads = 128;
+    // 384 x 128 until the caller sets a tiling: the best on GB300 where most water
+    // is at rest (2^26 basin 1.16e10 against 1.07e10 at 512; 2^22 adjoint step
+    // 1.15 against 1.17 ms), within 2 % of 512 where it moves (2^22 bowls).
+    // Meshes below 2^20 cells get 256-cell segments: with more cells per segment a
+    // 2^18-cell mesh has too few segments for the ~600 resident CTAs, and a step
+    // takes two segment-times (measured at 2^18: forward step 0.170 -> 0.145 ms,
+    // adjoint step 0.242 -> 0.222 ms against 512).
+    int32_t seg_cells = 384, block_threads = 128;
     bool tiling_set = false;
     int32_t stage_depth = 1;                        // segments staged ahead per CTA (1 or 2)
     int32_t arith = SWE_ARITH_STRICT;
@@ -579,7 +581,7 @@ int upload_meshes(swe_ctx* c, int64_t ni, const int64_t* n_cells, const int64_t*
     c->offset.swap(offset);
     c->cells_total = off;
     c->cells_packed = pc;
-    if (!c->tiling_set) c->seg_cells = off < ((int64_t)1 << 20) ? 256 : 512;
+    if (!c->tiling_set) c->seg_cells = off < ((int64_t)1 << 20) ? 256 : 384;
     c->max_ndepth = max_nd;
     swe_params p0 = c->params.empty() ? swe_params{} : c->params[0];
     c->params.assign((size_t)ni, p0);
