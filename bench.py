@@ -712,11 +712,20 @@ def run_gpu(a, rank, world, local):
                                        device="cuda")
         sg = sample.grid
         best, res = autotune.autotune(sg.mesh, sg.h, sg.hu, sg.hv, sg.b, sample.cfg.params(), sg.r_dt, device=local)
+        tuning = {"sample_cells": sg.mesh.n_cells, "sample_best": list(best),
+                  "ms_per_step": {"%dx%d/s%d" % k: round(v * 1e3, 4) for k, v in sorted(res.items())}}
+        del sample, sg
+        if a.tune_log2_cells < a.log2_cells:
+            # the sample's best few, timed again on the workload itself: tail effects differ
+            # between sizes, and near-ties on the sample need not be ties on the workload
+            top = sorted(res, key=res.get)[:4]
+            best, res2 = autotune.autotune(g.mesh, g.h, g.hu, g.hv, g.b, scn.cfg.params(), g.r_dt, device=local,
+                                           candidates=top)
+            tuning["workload_ms_per_step"] = {"%dx%d/s%d" % k: round(v * 1e3, 4) for k, v in sorted(res2.items())}
+        tuning["best"] = list(best)
         ctx.set_staging(1)
         ctx.set_tiling(best[0], best[1])
         ctx.set_staging(best[2])
-        tuning = {"sample_cells": sg.mesh.n_cells, "best": list(best),
-                  "ms_per_step": {"%dx%d/s%d" % k: round(v * 1e3, 4) for k, v in sorted(res.items())}}
     ctx.upload_mesh(g.mesh)
     ctx.upload_state(g.h, g.hu, g.hv, g.b)
     ctx.set_time(g.r_time, g.r_dt)

@@ -18,9 +18,11 @@ DEFAULT_STAGING = (1, 2)
 
 
 def autotune(mesh, h, hu, hv, b, params, dt, segments=DEFAULT_SEGMENTS, threads=DEFAULT_THREADS, steps=4,
-             device=0, staging=DEFAULT_STAGING):
+             device=0, staging=DEFAULT_STAGING, candidates=None):
     """Return ((segment_cells, block_threads, staging_depth), {setting: seconds per
-    step}) for the fastest setting of segment length, block size and staging depth."""
+    step}) for the fastest setting of segment length, block size and staging depth
+    (every combination, or the given (segment_cells, block_threads, staging_depth)
+    candidates, e.g. the best few of a search on a smaller sample)."""
     import torch
     ctx = swe.SweContext(device)
     results = {}
@@ -29,7 +31,9 @@ def autotune(mesh, h, hu, hv, b, params, dt, segments=DEFAULT_SEGMENTS, threads=
         ctx.upload_mesh(mesh)
         stream = torch.cuda.Stream(device=device)
         ctx.set_stream(stream.cuda_stream)
-        for depth, seg, thr in itertools.product(staging, segments, threads):
+        settings = [(d, sg, t) for sg, t, d in candidates] if candidates else \
+            list(itertools.product(staging, segments, threads))
+        for depth, seg, thr in settings:
             try:
                 ctx.set_staging(1)
                 ctx.set_tiling(seg, thr)
